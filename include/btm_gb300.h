@@ -1,0 +1,230 @@
+/*
+ * btm_gb300.h - C ABI of the GB300-native incompressible SIMPLE / SST k-omega
+ * forward model G(x, theta).
+ *
+ * Plain C: fixed-width integers, plain pointers and sizes, no exceptions and no
+ * torch types cross this boundary.  Every entry point returns an int status
+ * (BTM_OK = 0, negative = error; btm_last_error() gives the message) except the
+ * destroy calls.  All arrays are caller-owned host memory unless a name says
+ * "device".  Arithmetic is IEEE FP64 throughout the plain drop-in path.
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the reference project root):
+ *   - the case (mesh + boundary conditions + viscosity + settings) replaces the
+ *     constructor arguments of ForwardModel / SIMPLESolver
+ *     (incompressible/include/ForwardModel.hpp:78-90,
+ *      incompressible/include/SIMPLESolver.hpp:18-22);
+ *   - btm_solve replaces SIMPLESolver::initUniform + SIMPLESolver::solve as
+ *     called by ForwardModel::evaluate (incompressible/src/ForwardModel.cpp:41-89,
+ *     incompressible/src/SIMPLESolver.cpp:23-51, 696-1043);
+ *   - btm_solve_batch has no single reference counterpart: it replaces the
+ *     process-pool fan-out of independent evaluate() calls
+ *     (python/parallel_mcmc.py:37-57, python/UQ/datasets/channel_calibration.py:189-222).
+ */
+#ifndef BTM_GB300_H
+#define BTM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BTM_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+#define BTM_OK              0
+#define BTM_ERR_ARG        -1   /* invalid argument (sizes, null pointers, types) */
+#define BTM_ERR_CUDA       -2   /* a CUDA runtime call failed                     */
+#define BTM_ERR_NOMEM      -3   /* device or host allocation failed               */
+#define BTM_ERR_NODEVICE   -4   /* no CUDA device visible                         */
+#define BTM_ERR_TIMEOUT    -5   /* a bounded device-side wait ran out             */
+#define BTM_ERR_INTERNAL   -6
+
+/* ---- solve outcome: the reference EvaluationStatus
+ *      (core/include/EvaluationTypes.hpp:6-12, python/Bindings.cpp:276-281) ---- */
+#define BTM_CONVERGED           0
+#define BTM_UNCONVERGED         1
+#define BTM_DIVERGED            2
+#define BTM_INVALID_PARAMETERS  3
+#define BTM_UNKNOWN             4
+
+/* ---- boundary-condition kinds: the reference BCType
+ *      (core/include/BoundaryCondition.hpp:12-18), same order ---------------- */
+#define BTM_BC_DIRICHLET        0
+#define BTM_BC_NEUMANN          1
+#define BTM_BC_INLET_VELOCITY   2
+#define BTM_BC_OUTLET_PRESSURE  3
+#define BTM_BC_WALL_NO_SLIP     4
+#define BTM_BC_WALL_KOMEGA      5
+#define BTM_BC_WALL_MOVING      6
+#define BTM_BC_SYMMETRY         7
+#define BTM_BC_CYCLIC           8
+
+/* ---- patch types: Patch::type strings (core/include/Mesh.hpp:75-80) -------- */
+#define BTM_PATCH_OTHER    0
+#define BTM_PATCH_WALL     1
+#define BTM_PATCH_INLET    2
+#define BTM_PATCH_OUTLET   3
+#define BTM_PATCH_SYMMETRY 4
+
+/* ---- linear solver names (core/include/LinearSolver.hpp:659-665) ---------- */
+#define BTM_LS_PCG          0
+#define BTM_LS_BICGSTAB     1
+#define BTM_LS_GAUSSSEIDEL  2
+#define BTM_LS_AMG          3
+
+/* ---- SST closure variants (core/include/SSTModel.hpp:48) ------------------- */
+#define BTM_SST_FULL        0
+#define BTM_SST_NOLIMITER   1
+#define BTM_SST_KOMEGA      2
+
+/* Unstructured finite-volume mesh with precomputed geometry, the data a
+ * reference Mesh holds (core/include/Mesh.hpp:44-198).  Faces [0, n_internal)
+ * are internal (owner and neighbour cells), faces [n_internal, n_faces) are
+ * boundary faces (neighbour = -1).  Vectors are stored xyz-interleaved. */
+typedef struct btm_mesh {
+    int32_t n_cells;
+    int32_t n_faces;
+    int32_t n_internal_faces;
+    int32_t n_patches;
+    const int32_t *owner;          /* [n_faces]                                 */
+    const int32_t *neighbour;      /* [n_faces], -1 on boundary faces           */
+    const double  *face_center;    /* [n_faces*3]                               */
+    const double  *face_normal;    /* [n_faces*3] unit, outward from the owner  */
+    const double  *face_area;      /* [n_faces]                                 */
+    const double  *face_delta;     /* [n_faces] owner-to-neighbour distance     */
+    const double  *face_d;         /* [n_faces*3] owner-to-neighbour vector     */
+    const double  *face_weight;    /* [n_faces] phi_f = w phi_O + (1-w) phi_N   */
+    const double  *cell_center;    /* [n_cells*3]                               */
+    const double  *cell_volume;    /* [n_cells]                                 */
+    const double  *wall_distance;  /* [n_cells]                                 */
+    const int32_t *patch_type;     /* [n_patches] BTM_PATCH_*                   */
+    const int32_t *patch_offset;   /* [n_patches+1] into patch_faces            */
+    const int32_t *patch_faces;    /* [patch_offset[n_patches]] face ids        */
+} btm_mesh;
+
+/* Boundary conditions of one patch for the four solved fields: the reference
+ * PatchBC of velocityBC/pressureBC/kBC/omegaBC
+ * (core/include/BoundaryCondition.hpp:20-41).  Profiles, when non-null, hold
+ * one value per patch face in patch-face order (3 per face for velocity). */
+typedef struct btm_patch_bc {
+    int32_t u_type, p_type, k_type, omega_type;   /* BTM_BC_* */
+    double  u_value[3];
+    double  p_value;
+    double  k_value;
+    double  omega_value;
+    const double *u_profile;       /* [n_patch_faces*3] or NULL */
+    const double *k_profile;       /* [n_patch_faces]   or NULL */
+    const double *omega_profile;   /* [n_patch_faces]   or NULL */
+} btm_patch_bc;
+
+/* SIMPLE controls: the reference SolverSettings (core/include/FlowFields.hpp:53-132)
+ * restricted to the fields the incompressible solve reads. */
+typedef struct btm_settings {
+    int32_t max_iterations;
+    double  convergence_tol;
+    double  divergence_limit;
+    double  alpha_u, alpha_p, alpha_k, alpha_omega;
+    int32_t inner_iterations;
+    double  inner_tolerance;
+    int32_t turb_start_iter;
+    int32_t turb_update_interval;
+    int32_t nut_floor_iters;
+    int32_t rhie_chow_all_meshes;
+    double  body_force[3];
+    double  k_min, k_max, omega_min;
+    int32_t use_wall_functions;
+    double  von_karman;
+    double  wall_fn_E;
+    int32_t pressure_solver;       /* BTM_LS_* */
+    int32_t momentum_solver;
+    int32_t turbulence_solver;
+} btm_settings;
+
+/* Initial state.  mode 0 = cold uniform start exactly as
+ * SIMPLESolver::initUniform (SIMPLESolver.cpp:23-51); mode 1 = warm start from
+ * the fields in `warm` (a state previously returned by a solve, as the
+ * WarmStartCache does, ForwardModel.cpp:56-63). */
+typedef struct btm_state btm_state;
+typedef struct btm_init {
+    int32_t mode;
+    double  u[3];
+    double  p, k, omega;
+    const btm_state *warm;
+} btm_init;
+
+/* Full flow state: FlowFields (core/include/FlowFields.hpp:9-33).  Cell arrays
+ * have n_cells entries (U: n_cells*3), boundary arrays n_faces-n_internal
+ * entries (Ub: *3).  Any pointer may be NULL on output to skip that field. */
+struct btm_state {
+    double *U, *p, *k, *omega, *nuT, *F1, *F2, *Pk, *CDkw;
+    double *Ub, *pb, *kb, *omegab;
+    int32_t turb_established;
+};
+
+/* Convergence record: ConvergenceHistory (FlowFields.hpp:36-49).  The
+ * per-iteration residual arrays are optional (capacity 0 = not recorded);
+ * each entry is {Ux, Uy, Uz, p, k, omega} as ResidualEntry. */
+typedef struct btm_history {
+    int32_t status;                /* BTM_CONVERGED / UNCONVERGED / DIVERGED  */
+    int32_t converged;
+    int32_t diverged;
+    int32_t final_iter;            /* hist.finalIter                           */
+    int32_t iterations_run;        /* outer iterations executed                */
+    int64_t inner_iterations;      /* sum of all linear-solver iterations      */
+    double  last_residual[6];      /* last ResidualEntry                       */
+    int32_t residual_capacity;     /* rows available in `residuals`            */
+    double *residuals;             /* [residual_capacity*6] or NULL            */
+} btm_history;
+
+typedef struct btm_case btm_case;
+
+/* Last error message of the calling thread ("" if none). */
+const char *btm_last_error(void);
+int btm_abi_version(void);
+
+/* Build a device-resident case: mesh connectivity as SoA arrays, cell-to-face
+ * gather lists, the pressure AMG hierarchy (aggregation, Galerkin sparsity,
+ * colouring) and per-face boundary-condition codes.  `bcs` has n_patches
+ * entries.  Replaces ForwardModel/SIMPLESolver construction. */
+int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu,
+                    const btm_settings *settings, btm_case **out);
+void btm_case_destroy(btm_case *c);
+int btm_case_info(const btm_case *c, int32_t *n_cells, int32_t *n_boundary_faces,
+                  int32_t *n_amg_levels, int32_t *is_2d);
+
+/* One forward solve on the device.  coeffs[11] are the SST constants in the
+ * InferenceParameterSet order (core/include/InferenceParameters.hpp:11-14);
+ * variant is BTM_SST_*.  `out` and `hist` may be NULL. */
+int btm_solve(btm_case *c, const double *coeffs, int32_t variant,
+              const btm_init *init, btm_state *out, btm_history *hist);
+
+/* n independent solves in one persistent launch (one CTA per instance when the
+ * mesh is small enough).  cases[i] may repeat.  coeffs is n*11, variants n,
+ * inits n; outs/hists may be NULL or arrays of n. */
+int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs,
+                    const int32_t *variants, const btm_init *inits,
+                    btm_state *outs, btm_history *hists);
+
+/* ---- test hooks (no reference counterpart): run one phase of the engine
+ * on the device for parity tests against the oracle.  Inputs/outputs are host
+ * arrays sized as documented per phase in the engine source. ---------------- */
+#define BTM_PHASE_GRAD          1   /* greenGaussGrad                         */
+#define BTM_PHASE_SST           2   /* SSTModel::computeFields + |S|           */
+#define BTM_PHASE_MOMENTUM      3   /* assembleMomentum (one component)        */
+#define BTM_PHASE_PRESSURE      4   /* assemblePressureCorrection              */
+#define BTM_PHASE_KEQ           5   /* assembleKEquation                       */
+#define BTM_PHASE_OMEGAEQ       6   /* assembleOmegaEquation                   */
+#define BTM_PHASE_SPMV          7   /* LinearSystem::matvec                    */
+#define BTM_PHASE_BICGSTAB      8   /* BiCGSTABSolver::solve                   */
+#define BTM_PHASE_AMGPCG        9   /* AMG-preconditioned CG                   */
+#define BTM_PHASE_ITER         10   /* N full SIMPLE outer iterations          */
+int btm_debug_phase(btm_case *c, int32_t phase, const double *coeffs,
+                    int32_t variant, int32_t arg, const double *in, int64_t n_in,
+                    double *out, int64_t n_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BTM_GB300_H */

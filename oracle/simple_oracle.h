@@ -1,0 +1,58 @@
+/*
+ * simple_oracle.h - plain-C restatement of the reference incompressible
+ * SIMPLE / SST k-omega solver (TEST INFRASTRUCTURE ONLY: the checker for the
+ * GB300 kernels; never linked into the product).
+ *
+ * Inputs and outputs use the structs of include/btm_gb300.h.  Every function
+ * follows the reference operation order so that, with floating-point
+ * contraction disabled, results are bit-identical to the reference build.
+ */
+#ifndef SIMPLE_ORACLE_H
+#define SIMPLE_ORACLE_H
+
+#include "../include/btm_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Full solve: SIMPLESolver::initUniform (or warm state) + SIMPLESolver::solve
+ * (incompressible/src/SIMPLESolver.cpp:23-51, 696-1043).  Returns 0. */
+int oracle_solve(const btm_mesh *m, const btm_patch_bc *bcs, double nu, const btm_settings *s,
+                 const double *coeffs, int variant, const btm_init *init, btm_state *out,
+                 btm_history *hist);
+
+/* greenGaussGrad (core/include/Field.hpp:122-152): grad is n_cells*3. */
+void oracle_green_gauss(const btm_mesh *m, const double *phi, const double *phib, double *grad);
+
+/* SSTModel::computeFields + strainRateMagnitude (core/src/SSTModel.cpp:122-172,
+ * core/include/Field.hpp:232-267).  U/Ub are xyz-interleaved. */
+void oracle_sst_fields(const btm_mesh *m, const double *coeffs, int variant, double nu,
+                       const double *U, const double *Ub, const double *k, const double *kb,
+                       const double *om, const double *omb, double *nuT, double *F1, double *F2,
+                       double *Pk, double *CDkw, double *Smag);
+
+/* Assembly of one linear system from a state.  kind: 0/1/2 = momentum
+ * component x/y/z (SIMPLESolver.cpp:56-203), 3 = pressure correction with
+ * aP taken from `aP` (:322-450), 4 = k (:483-560), 5 = omega with frozen
+ * Smag (:567-669).  Outputs diag/source [n_cells], upper/lower [n_internal];
+ * for momentum also aP_out [n_cells] (relaxed diagonal). */
+void oracle_assemble(const btm_mesh *m, const btm_patch_bc *bcs, double nu,
+                     const btm_settings *s, const double *coeffs, int kind,
+                     const btm_state *st, const double *aP, const double *Smag,
+                     double *diag, double *upper, double *lower, double *source, double *aP_out);
+
+/* LinearSystem::matvec (core/include/LinearSolver.hpp:68-77). */
+void oracle_matvec(int nC, int nIF, const int *own, const int *nbr, const double *diag,
+                   const double *upper, const double *lower, const double *x, double *y);
+
+/* ILinearSolver::solve for solver code BTM_LS_*; res[0..3] = iterations,
+ * finalRes, initialRes, converged (LinearSolver.hpp:99-111). */
+void oracle_linear_solve(int kind, int nC, int nIF, const int *own, const int *nbr,
+                         const double *diag, const double *upper, const double *lower,
+                         const double *source, double *x, int max_iter, double tol, double *res);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
