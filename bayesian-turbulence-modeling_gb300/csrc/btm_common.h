@@ -1,0 +1,134 @@
+// btm_common.h - data layout shared by the host driver (btm_host.cpp) and the
+// device engine (btm_engine.cu).  Plain structs of device pointers; one
+// DevMesh per case (read-only after creation), one DevInst per solve instance.
+#pragma once
+#include <stdint.h>
+
+namespace btm {
+
+constexpr int kMaxLevels = 20;       // AMG levels (reference cap, LinearSolver.hpp:508)
+constexpr int kCoarseDirect = 32;    // coarsest level at or below this size: dense inverse
+constexpr int kCoarseSweeps = 50;    // GS sweeps when the coarsest level is larger
+constexpr int kRedSlots = 4;         // values per fused team reduction
+
+// Boundary-condition codes per boundary face (resolved on the host from the
+// per-patch btm_patch_bc list in patch order, last patch wins).
+enum : int32_t {
+    BC_NONE = -1,        // face in no patch: boundary value left untouched
+    BC_ZEROGRAD = 0,     // value = owner cell value
+    BC_FIXED = 1,        // value = stored per-face value
+    BC_SYMMETRY = 2,     // velocity only: Uo - n (Uo.n)
+    BC_WALL_OMEGA = 3,   // omega only: 60 nu / (beta1 delta^2)
+};
+
+struct AmgLevelDev {
+    int32_t n;            // rows of this level
+    int32_t nnz;          // CSR entries (levels >= 1)
+    const int32_t *rowPtr, *colIdx, *diagPos;     // CSR (levels >= 1)
+    const int32_t *gOff, *gIdx;                   // Galerkin gather into the finer level's values
+    const int32_t *map;                           // this level's rows -> next level's rows
+    const int32_t *aggOff, *aggMem;               // next level's rows -> members here (ascending)
+    int32_t nColors;
+    const int32_t *colorOff, *colorRows;          // rows grouped by colour
+    int64_t valOff;       // offset of this level's values in DevInst::amgVal (levels >= 1)
+    int64_t vecOff;       // offset of this level's x/b/r in DevInst::amgX/amgB/amgR (levels >= 1)
+};
+
+struct DevMesh {
+    int32_t nC, nIF, nB, nF;
+    int32_t is2d;          // all normals z == 0: the z-momentum system is identically zero
+    int32_t hasOutlet;     // a non-empty outlet patch exists
+    int32_t rhieChow;      // Rhie-Chow dissipation active (no outlet, or forced)
+    int32_t maxCellFaces;
+    // internal faces [nIF]
+    const int32_t *own, *nbr;
+    const double *w, *area, *deltaC;              // deltaC = max(delta, 1e-20)
+    const double *nx, *ny, *nz, *sfx, *sfy, *sfz; // unit normal, n * area
+    const double *ex, *ey, *ez;                   // d / max(delta, 1e-30)
+    // boundary faces [nB] (index b = face - nIF)
+    const int32_t *bown;
+    const double *barea, *bdeltaC, *bdeltaW;      // bdeltaW = max(delta, 1e-20) for omega wall BC
+    const double *bnx, *bny, *bnz, *bsfx, *bsfy, *bsfz;
+    const int32_t *bwall;                         // face belongs to a 'wall' patch
+    const int32_t *bout;                          // face belongs to an 'outlet' patch
+    const int32_t *bcU, *bcP, *bcK, *bcW;         // BC codes (BC_*) per face
+    const int32_t *bcPp;                          // p' boundary rule: 0 copy owner, 1 keep zero
+    const double *bvUx, *bvUy, *bvUz, *bvP, *bvK, *bvW;
+    // cells [nC]
+    const double *vol, *wd;
+    const int32_t *cfOff;      // [nC+1] internal-face gather list, ascending face index
+    const int32_t *cfFace;     // face index
+    const int32_t *cfOther;    // other cell, negated-1 when this cell is the neighbour: other = -(x+1)
+    const int32_t *cbOff;      // [nC+1] boundary faces, ascending face index (b indices)
+    const int32_t *cbFace;
+    const int32_t *cbpOff;     // [nC+1] boundary faces in patch iteration order
+    const int32_t *cbpFace;
+    const int32_t *pinFace;    // [nC] boundary index of the last wall face (patch order), or -1
+    // pressure AMG hierarchy
+    int32_t nLevels;
+    int32_t coarseDirect;      // coarsest level solved by its dense inverse
+    AmgLevelDev lev[kMaxLevels];
+    int64_t amgValTotal, amgVecTotal;
+};
+
+// Scalar controls of one solve (SolverSettings fields read by the loop).
+struct DevSettings {
+    int32_t maxIter, innerIter, turbStart, turbInterval, nutFloorIters, useWallFn;
+    int32_t momSolver, turbSolver, pSolver;
+    double convTol, divLimit, alphaU, alphaP, alphaK, alphaW, innerTol;
+    double bodyForce[3];
+    double kMin, kMax, omegaMin, vonKarman;
+};
+
+struct DevInst {
+    const DevMesh *M;      // device pointer
+    DevSettings S;
+    double nu;
+    double coeff[11];
+    int32_t variant;
+    int32_t initMode;      // 0 cold uniform, 1 warm (fields already uploaded)
+    double init[6];        // Ux, Uy, Uz, p, k, omega for a cold start
+    int32_t solveZ;        // 0 when the z-momentum system is identically zero
+    // state [nC] / [nB]
+    double *ux, *uy, *uz, *p, *k, *om, *nut, *f1, *f2, *pk, *cdkw;
+    double *ubx, *uby, *ubz, *pb, *kb, *omb;
+    // work [nC]
+    double *smag, *gpx, *gpy, *gpz;
+    double *g[9];          // velocity gradients: dU_i/dx_j at g[3*i+j]
+    // linear system: diag [nC] | upper [nIF] | lower [nIF] contiguous, so the
+    // pressure Galerkin gather indexes one array (diag i, upper nC+f, lower nC+nIF+f)
+    double *diag, *upper, *lower;
+    double *src, *aPx, *pp, *kold, *omold;
+    double *r, *rh, *pv, *v, *s, *t, *ph, *sh;
+    double *rd;            // [nC] reciprocal Jacobi diagonal of the system being solved
+    double *fflux;         // [nIF] per-face flux scratch
+    double *ppb;           // [nB] p' boundary values
+    // AMG per-instance values and vectors
+    double *amgVal, *amgX, *amgB, *amgR;
+    double *amgRd;         // [nC + amgVecTotal] Gauss-Seidel reciprocal diagonals per level
+    double *ainv, *gj;     // dense inverse [nc*nc], Gauss-Jordan ping-pong [2*nc*2nc]
+    // grid-team reduction partials [2][gridDim][kRedSlots] and barrier words
+    double *gpart;
+    unsigned int *barrier;  // [2]: arrival count, generation
+    int32_t *err;           // error flag (nonzero: abort)
+    // outputs
+    int32_t *out;           // [8]: status, converged, diverged, finalIter, itersRun, turbEst, _, _
+    int64_t *outInner;      // [1] total inner iterations
+    uint64_t *outTime;      // [8] ns per phase (leader thread's globaltimer)
+    double *outLast;        // [6] last residual entry
+    double *hist;           // [histCap*6] or null
+    int32_t histCap;
+    int32_t turbEstIn;      // turbEstablished of a warm state
+    // debug phase I/O (test hooks)
+    int32_t dbgPhase, dbgArg;
+    double *dbgIn, *dbgOut;
+};
+
+// engine entry points (btm_engine.cu)
+int engine_block_threads();
+int engine_launch_block(DevInst *dInsts, int n, void *stream);
+int engine_launch_grid(DevInst *dInst, int blocks, void *stream);
+int engine_grid_blocks(int *blocks_out);
+int engine_launch_debug(DevInst *dInst, void *stream);
+
+}  // namespace btm

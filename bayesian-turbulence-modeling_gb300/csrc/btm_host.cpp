@@ -1,0 +1,1039 @@
+// btm_host.cpp - host driver of the GB300 SIMPLE / SST engine and the C ABI
+// declared in include/btm_gb300.h.
+//
+// A case (mesh + BCs + viscosity + settings) is preprocessed once into
+// device-resident structure-of-arrays: internal/boundary face data, per-cell
+// face gather lists in ascending face order (the order in which the
+// reference's face loops reach each cell), per-face boundary-condition codes,
+// and the pressure AMG hierarchy (aggregation, Galerkin gather lists,
+// colouring).  Solves reuse per-case instance slabs; each solve is one
+// persistent launch (btm_engine.cu).
+#include "btm_common.h"
+
+#include "../../include/btm_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+
+struct BtmError : std::runtime_error {
+    int code;
+    BtmError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess)
+        throw BtmError(BTM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+// ---------------------------------------------------------------------------
+// device arena: one allocation, 256-byte aligned sub-arrays
+// ---------------------------------------------------------------------------
+struct Arena {
+    std::vector<char> host;
+    size_t off = 0;
+    template <class T>
+    size_t put(const T *src, size_t n) {
+        off = (off + 255) & ~size_t(255);
+        size_t at = off;
+        size_t bytes = n * sizeof(T);
+        if (host.size() < off + bytes + 256) host.resize(std::max(host.size() * 2, off + bytes + 256));
+        if (bytes) std::memcpy(host.data() + off, src, bytes);
+        off += bytes;
+        return at;
+    }
+    template <class T>
+    size_t put(const std::vector<T> &v) { return put(v.data(), v.size()); }
+};
+
+// ---------------------------------------------------------------------------
+// AMG setup (host, once per case)
+// ---------------------------------------------------------------------------
+struct HLevel {
+    int n = 0;
+    // CSR with rows sorted by column; entry ids index the level's value array
+    // (level 0: the LDU array diag|upper|lower; coarser: CSR positions)
+    std::vector<int> rowPtr, colIdx, entry, diagPos;
+    std::vector<double> val;   // geometric values (aggregation only)
+    std::vector<int> map;      // -> next level
+    int nCoarse = 0;
+    std::vector<int> aggOff, aggMem;
+    std::vector<int> gOff, gIdx;  // Galerkin gather of this level's entries (levels >= 1)
+    std::vector<int> colorOff, colorRows;
+    int nColors = 0;
+};
+
+// buildAggregates (core/include/LinearSolver.hpp:407-443), applied to the
+// geometric pressure Laplacian: greedy seeds with strength > 0.25, then
+// orphans join their strongest aggregated neighbour.
+int aggregate(const HLevel &L, std::vector<int> &map) {
+    const int n = L.n;
+    map.assign(n, -1);
+    std::vector<double> diag(n, 0.0);
+    for (int i = 0; i < n; ++i)
+        if (L.diagPos[i] >= 0) diag[i] = L.val[L.diagPos[i]];
+    int nCoarse = 0;
+    for (int i = 0; i < n; ++i) {
+        if (map[i] >= 0) continue;
+        int agg = nCoarse++;
+        map[i] = agg;
+        double aii = std::abs(diag[i]);
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j) {
+            int c = L.colIdx[j];
+            if (c == i || map[c] >= 0) continue;
+            double ajj = std::abs(diag[c]);
+            double strength = std::abs(L.val[j]) / std::sqrt(aii * ajj + 1e-30);
+            if (strength > 0.25) map[c] = agg;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        if (map[i] >= 0) continue;
+        double bestStr = -1.0;
+        int bestAgg = 0;
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j) {
+            int c = L.colIdx[j];
+            if (c == i && map[c] < 0) continue;
+            if (map[c] >= 0 && std::abs(L.val[j]) > bestStr) {
+                bestStr = std::abs(L.val[j]);
+                bestAgg = map[c];
+            }
+        }
+        map[i] = bestAgg;
+    }
+    return nCoarse;
+}
+
+// Galerkin product A_c = P^T A P for piecewise-constant P: builds the coarse
+// CSR, its geometric values and, per coarse entry, the list of fine entry ids
+// that sum into it (members ascending, then fine columns ascending).
+void galerkin(HLevel &F, HLevel &C) {
+    const int nc = F.nCoarse;
+    C.n = nc;
+    F.aggOff.assign(nc + 1, 0);
+    for (int i = 0; i < F.n; ++i) F.aggOff[F.map[i] + 1]++;
+    for (int I = 0; I < nc; ++I) F.aggOff[I + 1] += F.aggOff[I];
+    F.aggMem.assign(F.n, 0);
+    std::vector<int> cur(F.aggOff.begin(), F.aggOff.end() - 1);
+    for (int i = 0; i < F.n; ++i) F.aggMem[cur[F.map[i]]++] = i;
+
+    C.rowPtr.assign(nc + 1, 0);
+    C.colIdx.clear(); C.val.clear(); C.gOff.assign(1, 0); C.gIdx.clear();
+    std::vector<int> marker(nc, -1), slot(nc, 0);
+    std::vector<std::vector<int>> lists;
+    std::vector<int> cols;
+    std::vector<double> vals;
+    for (int I = 0; I < nc; ++I) {
+        cols.clear(); vals.clear(); lists.clear();
+        for (int q = F.aggOff[I]; q < F.aggOff[I + 1]; ++q) {
+            int i = F.aggMem[q];
+            for (int j = F.rowPtr[i]; j < F.rowPtr[i + 1]; ++j) {
+                int J = F.map[F.colIdx[j]];
+                if (marker[J] != I) {
+                    marker[J] = I;
+                    slot[J] = (int)cols.size();
+                    cols.push_back(J);
+                    vals.push_back(0.0);
+                    lists.emplace_back();
+                }
+                vals[slot[J]] += F.val[j];
+                lists[slot[J]].push_back(F.entry[j]);
+            }
+        }
+        std::vector<int> order(cols.size());
+        for (size_t e = 0; e < order.size(); ++e) order[e] = (int)e;
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return cols[a] < cols[b]; });
+        for (int e : order) {
+            C.colIdx.push_back(cols[e]);
+            C.val.push_back(vals[e]);
+            for (int id : lists[e]) C.gIdx.push_back(id);
+            C.gOff.push_back((int)C.gIdx.size());
+        }
+        C.rowPtr[I + 1] = (int)C.colIdx.size();
+    }
+    C.entry.resize(C.colIdx.size());
+    for (size_t e = 0; e < C.entry.size(); ++e) C.entry[e] = (int)e;
+    C.diagPos.assign(nc, -1);
+    for (int I = 0; I < nc; ++I)
+        for (int j = C.rowPtr[I]; j < C.rowPtr[I + 1]; ++j)
+            if (C.colIdx[j] == I) C.diagPos[I] = j;
+}
+
+// Colouring for the multicolour Gauss-Seidel smoother: a two-colouring when
+// the graph is bipartite (quad meshes), else greedy in row order.
+void colour(HLevel &L) {
+    const int n = L.n;
+    std::vector<int> col(n, -1);
+    bool bip = true;
+    std::deque<int> q;
+    for (int s = 0; s < n && bip; ++s) {
+        if (col[s] >= 0) continue;
+        col[s] = 0;
+        q.push_back(s);
+        while (!q.empty() && bip) {
+            int i = q.front();
+            q.pop_front();
+            for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j) {
+                int c = L.colIdx[j];
+                if (c == i) continue;
+                if (col[c] < 0) { col[c] = 1 - col[i]; q.push_back(c); }
+                else if (col[c] == col[i]) { bip = false; break; }
+            }
+        }
+    }
+    if (!bip) {
+        col.assign(n, -1);
+        std::vector<int> mark;
+        for (int i = 0; i < n; ++i) {
+            mark.assign(mark.size(), 0);
+            for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j) {
+                int c = L.colIdx[j];
+                if (c != i && col[c] >= 0) {
+                    if ((int)mark.size() <= col[c]) mark.resize(col[c] + 1, 0);
+                    mark[col[c]] = 1;
+                }
+            }
+            int k = 0;
+            while (k < (int)mark.size() && mark[k]) ++k;
+            col[i] = k;
+            if ((int)mark.size() <= k) mark.resize(k + 1, 0);
+        }
+    }
+    int nColors = 0;
+    for (int c : col) nColors = std::max(nColors, c + 1);
+    L.nColors = nColors;
+    L.colorOff.assign(nColors + 1, 0);
+    for (int c : col) L.colorOff[c + 1]++;
+    for (int c = 0; c < nColors; ++c) L.colorOff[c + 1] += L.colorOff[c];
+    L.colorRows.assign(n, 0);
+    std::vector<int> cur(L.colorOff.begin(), L.colorOff.end() - 1);
+    for (int i = 0; i < n; ++i) L.colorRows[cur[col[i]]++] = i;
+}
+
+// ---------------------------------------------------------------------------
+// case and instance objects
+// ---------------------------------------------------------------------------
+struct Slab {
+    void *dptr = nullptr;
+    size_t bytes = 0;
+    btm::DevInst inst{};   // host copy with device pointers
+};
+
+}  // namespace
+
+struct btm_case {
+    int nC = 0, nIF = 0, nB = 0, nF = 0, nP = 0;
+    double nu = 0.0;
+    btm_settings settings{};
+    bool is2d = false, bcZeroZ = true;
+    int maxGridBlocks = 0;
+    // device
+    void *meshArena = nullptr;
+    btm::DevMesh dmesh{};            // host copy with device pointers
+    btm::DevMesh *dMeshPtr = nullptr;
+    int amgCoarseN = 0;
+    int64_t amgValTotal = 0, amgVecTotal = 0;
+    std::vector<Slab> slabs;
+    std::mutex mtx;
+    cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+std::once_flag g_dev_once;
+int g_dev_status = 0;
+std::string g_dev_msg;
+
+int ensure_device() {
+    std::call_once(g_dev_once, [] {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n == 0) {
+            g_dev_status = BTM_ERR_NODEVICE;
+            g_dev_msg = std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+        }
+    });
+    if (g_dev_status) g_err = g_dev_msg;
+    return g_dev_status;
+}
+
+btm::DevSettings dev_settings(const btm_settings &s) {
+    btm::DevSettings d{};
+    d.maxIter = s.max_iterations;
+    d.innerIter = s.inner_iterations;
+    d.turbStart = s.turb_start_iter;
+    d.turbInterval = s.turb_update_interval;
+    d.nutFloorIters = s.nut_floor_iters;
+    d.useWallFn = s.use_wall_functions;
+    d.momSolver = s.momentum_solver;
+    d.turbSolver = s.turbulence_solver;
+    d.pSolver = s.pressure_solver;
+    d.convTol = s.convergence_tol;
+    d.divLimit = s.divergence_limit;
+    d.alphaU = s.alpha_u;
+    d.alphaP = s.alpha_p;
+    d.alphaK = s.alpha_k;
+    d.alphaW = s.alpha_omega;
+    d.innerTol = s.inner_tolerance;
+    for (int i = 0; i < 3; ++i) d.bodyForce[i] = s.body_force[i];
+    d.kMin = s.k_min;
+    d.kMax = s.k_max;
+    d.omegaMin = s.omega_min;
+    d.vonKarman = s.von_karman;
+    return d;
+}
+
+void check_settings(const btm_settings &s) {
+    if (s.turb_update_interval <= 0) throw BtmError(BTM_ERR_ARG, "turb_update_interval must be positive");
+    for (int code : {s.pressure_solver, s.momentum_solver, s.turbulence_solver}) {
+        if (code == BTM_LS_GAUSSSEIDEL)
+            throw BtmError(BTM_ERR_ARG, "the GaussSeidel linear solver is not available on the device");
+        if (code < 0 || code > 3) throw BtmError(BTM_ERR_ARG, "unknown linear solver code");
+    }
+    if (!(s.alpha_u > 0) || !(s.alpha_k > 0) || !(s.alpha_omega > 0))
+        throw BtmError(BTM_ERR_ARG, "relaxation factors must be positive");
+}
+
+void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
+    const int nC = m->n_cells, nF = m->n_faces, nIF = m->n_internal_faces, nP = m->n_patches;
+    if (nC <= 0 || nF < nIF || nIF < 0 || nP < 0) throw BtmError(BTM_ERR_ARG, "bad mesh sizes");
+    const int nB = nF - nIF;
+    C->nC = nC; C->nIF = nIF; C->nB = nB; C->nF = nF; C->nP = nP;
+    for (int f = 0; f < nF; ++f) {
+        int o = m->owner[f], n = m->neighbour[f];
+        if (o < 0 || o >= nC) throw BtmError(BTM_ERR_ARG, "face owner out of range");
+        if (f < nIF ? (n < 0 || n >= nC) : (n >= 0))
+            throw BtmError(BTM_ERR_ARG, "internal faces must come first and have a neighbour");
+    }
+    // patch membership: every boundary face in at most one patch
+    std::vector<int> facePatch(nB, -1), faceSlot(nB, -1);
+    for (int p = 0; p < nP; ++p)
+        for (int q = m->patch_offset[p]; q < m->patch_offset[p + 1]; ++q) {
+            int f = m->patch_faces[q];
+            if (f < nIF || f >= nF) throw BtmError(BTM_ERR_ARG, "patch face is not a boundary face");
+            if (facePatch[f - nIF] >= 0) throw BtmError(BTM_ERR_ARG, "boundary face listed in two patches");
+            facePatch[f - nIF] = p;
+            faceSlot[f - nIF] = q - m->patch_offset[p];
+        }
+
+    Arena A;
+    btm::DevMesh &D = C->dmesh;
+    std::memset(&D, 0, sizeof D);
+    D.nC = nC; D.nIF = nIF; D.nB = nB; D.nF = nF;
+    bool hasOutlet = false;
+    for (int p = 0; p < nP; ++p)
+        if (m->patch_type[p] == BTM_PATCH_OUTLET && m->patch_offset[p + 1] > m->patch_offset[p]) hasOutlet = true;
+    D.hasOutlet = hasOutlet;
+    D.rhieChow = (!hasOutlet || C->settings.rhie_chow_all_meshes) ? 1 : 0;
+    bool is2d = true;
+    for (int f = 0; f < nF; ++f)
+        if (m->face_normal[3 * f + 2] != 0.0) is2d = false;
+    C->is2d = is2d;
+    D.is2d = is2d;
+
+    // internal faces
+    std::vector<double> w(nIF), area(nIF), dC(nIF), nx(nIF), ny(nIF), nz(nIF), sx(nIF), sy(nIF), sz(nIF),
+        ex(nIF), ey(nIF), ez(nIF);
+    std::vector<int> own(nIF), nbr(nIF);
+    for (int f = 0; f < nIF; ++f) {
+        own[f] = m->owner[f]; nbr[f] = m->neighbour[f];
+        w[f] = m->face_weight[f];
+        area[f] = m->face_area[f];
+        double del = m->face_delta[f];
+        dC[f] = std::max(del, 1e-20);
+        nx[f] = m->face_normal[3 * f]; ny[f] = m->face_normal[3 * f + 1]; nz[f] = m->face_normal[3 * f + 2];
+        sx[f] = nx[f] * area[f]; sy[f] = ny[f] * area[f]; sz[f] = nz[f] * area[f];
+        double dd = std::max(del, 1e-30);
+        ex[f] = m->face_d[3 * f] / dd; ey[f] = m->face_d[3 * f + 1] / dd; ez[f] = m->face_d[3 * f + 2] / dd;
+    }
+    // boundary faces
+    std::vector<int> bown(nB), bwall(nB, 0), bout(nB, 0), bcU(nB, btm::BC_NONE), bcP(nB, btm::BC_NONE),
+        bcK(nB, btm::BC_NONE), bcW(nB, btm::BC_NONE), bcPp(nB, 1);
+    std::vector<double> barea(nB), bdC(nB), bdW(nB), bnx(nB), bny(nB), bnz(nB), bsx(nB), bsy(nB), bsz(nB),
+        bvUx(nB, 0.0), bvUy(nB, 0.0), bvUz(nB, 0.0), bvP(nB, 0.0), bvK(nB, 0.0), bvW(nB, 0.0);
+    bool bcZeroZ = true;
+    for (int b = 0; b < nB; ++b) {
+        int f = nIF + b;
+        bown[b] = m->owner[f];
+        barea[b] = m->face_area[f];
+        bdC[b] = std::max(m->face_delta[f], 1e-20);
+        bdW[b] = std::max(m->face_delta[f], 1e-20);
+        bnx[b] = m->face_normal[3 * f]; bny[b] = m->face_normal[3 * f + 1]; bnz[b] = m->face_normal[3 * f + 2];
+        bsx[b] = bnx[b] * barea[b]; bsy[b] = bny[b] * barea[b]; bsz[b] = bnz[b] * barea[b];
+        int p = facePatch[b];
+        if (p < 0) continue;
+        int kk = faceSlot[b];
+        int ptype = m->patch_type[p];
+        bwall[b] = ptype == BTM_PATCH_WALL;
+        bout[b] = ptype == BTM_PATCH_OUTLET;
+        bcPp[b] = ptype == BTM_PATCH_OUTLET ? 1 : 0;
+        const btm_patch_bc &bc = bcs[p];
+        switch (bc.u_type) {
+            case BTM_BC_WALL_NO_SLIP: bcU[b] = btm::BC_FIXED; break;
+            case BTM_BC_WALL_MOVING:
+                bcU[b] = btm::BC_FIXED;
+                bvUx[b] = bc.u_value[0]; bvUy[b] = bc.u_value[1]; bvUz[b] = bc.u_value[2];
+                break;
+            case BTM_BC_INLET_VELOCITY:
+            case BTM_BC_DIRICHLET:
+                bcU[b] = btm::BC_FIXED;
+                if (bc.u_profile) {
+                    bvUx[b] = bc.u_profile[3 * kk]; bvUy[b] = bc.u_profile[3 * kk + 1]; bvUz[b] = bc.u_profile[3 * kk + 2];
+                } else {
+                    bvUx[b] = bc.u_value[0]; bvUy[b] = bc.u_value[1]; bvUz[b] = bc.u_value[2];
+                }
+                break;
+            case BTM_BC_SYMMETRY: bcU[b] = btm::BC_SYMMETRY; break;
+            default: bcU[b] = btm::BC_ZEROGRAD; break;
+        }
+        if (bcU[b] == btm::BC_FIXED && bvUz[b] != 0.0) bcZeroZ = false;
+        if (bc.p_type == BTM_BC_OUTLET_PRESSURE || bc.p_type == BTM_BC_DIRICHLET) {
+            bcP[b] = btm::BC_FIXED; bvP[b] = bc.p_value;
+        } else {
+            bcP[b] = btm::BC_ZEROGRAD;
+        }
+        if (bc.k_type == BTM_BC_WALL_KOMEGA) { bcK[b] = btm::BC_FIXED; bvK[b] = 0.0; }
+        else if (bc.k_type == BTM_BC_DIRICHLET) { bcK[b] = btm::BC_FIXED; bvK[b] = bc.k_profile ? bc.k_profile[kk] : bc.k_value; }
+        else bcK[b] = btm::BC_ZEROGRAD;
+        if (bc.omega_type == BTM_BC_WALL_KOMEGA) bcW[b] = btm::BC_WALL_OMEGA;
+        else if (bc.omega_type == BTM_BC_DIRICHLET) { bcW[b] = btm::BC_FIXED; bvW[b] = bc.omega_profile ? bc.omega_profile[kk] : bc.omega_value; }
+        else bcW[b] = btm::BC_ZEROGRAD;
+    }
+    C->bcZeroZ = bcZeroZ;
+
+    // cell gather lists
+    std::vector<int> cfOff(nC + 1, 0), cbOff(nC + 1, 0), cbpOff(nC + 1, 0), pin(nC, -1);
+    for (int f = 0; f < nIF; ++f) { cfOff[own[f] + 1]++; cfOff[nbr[f] + 1]++; }
+    for (int c = 0; c < nC; ++c) cfOff[c + 1] += cfOff[c];
+    std::vector<int> cfFace(cfOff[nC]), cfOther(cfOff[nC]);
+    {
+        std::vector<int> cur(cfOff.begin(), cfOff.end() - 1);
+        for (int f = 0; f < nIF; ++f) {
+            int o = own[f], n = nbr[f];
+            cfFace[cur[o]] = f; cfOther[cur[o]++] = n;
+            cfFace[cur[n]] = f; cfOther[cur[n]++] = -(o + 1);
+        }
+    }
+    int maxCF = 0;
+    for (int c = 0; c < nC; ++c) maxCF = std::max(maxCF, cfOff[c + 1] - cfOff[c]);
+    for (int b = 0; b < nB; ++b) cbOff[bown[b] + 1]++;
+    for (int c = 0; c < nC; ++c) cbOff[c + 1] += cbOff[c];
+    std::vector<int> cbFace(std::max(1, cbOff[nC]));
+    {
+        std::vector<int> cur(cbOff.begin(), cbOff.end() - 1);
+        for (int b = 0; b < nB; ++b) cbFace[cur[bown[b]]++] = b;
+    }
+    for (int p = 0; p < nP; ++p)
+        for (int q = m->patch_offset[p]; q < m->patch_offset[p + 1]; ++q) cbpOff[m->owner[m->patch_faces[q]] + 1]++;
+    for (int c = 0; c < nC; ++c) cbpOff[c + 1] += cbpOff[c];
+    std::vector<int> cbpFace(std::max(1, cbpOff[nC]));
+    {
+        std::vector<int> cur(cbpOff.begin(), cbpOff.end() - 1);
+        for (int p = 0; p < nP; ++p)
+            for (int q = m->patch_offset[p]; q < m->patch_offset[p + 1]; ++q) {
+                int f = m->patch_faces[q];
+                cbpFace[cur[m->owner[f]]++] = f - nIF;
+                if (m->patch_type[p] == BTM_PATCH_WALL) pin[m->owner[f]] = f - nIF;
+            }
+    }
+    D.maxCellFaces = maxCF;
+
+    // ---- pressure AMG hierarchy on the geometric Laplacian ----------------
+    std::vector<HLevel> lv(1);
+    {
+        HLevel &L0 = lv[0];
+        L0.n = nC;
+        // LDU values with aP = 1: coefficient (w Vo + (1-w) Vn) A / delta
+        std::vector<double> diag(nC, 0.0), coef(nIF);
+        for (int f = 0; f < nIF; ++f) {
+            double dpf = w[f] * m->cell_volume[own[f]] + (1.0 - w[f]) * m->cell_volume[nbr[f]];
+            coef[f] = dpf * area[f] / dC[f];
+            diag[own[f]] += coef[f];
+            diag[nbr[f]] += coef[f];
+        }
+        for (int b = 0; b < nB; ++b)
+            if (bout[b]) diag[bown[b]] += m->cell_volume[bown[b]] * barea[b] / bdC[b];
+        if (!hasOutlet) diag[0] += std::abs(diag[0]) > 1e-30 ? diag[0] : 1.0;
+        // CSR rows sorted by column; entry ids into diag|upper|lower
+        L0.rowPtr.assign(nC + 1, 0);
+        for (int c = 0; c < nC; ++c) L0.rowPtr[c + 1] = L0.rowPtr[c] + 1 + (cfOff[c + 1] - cfOff[c]);
+        L0.colIdx.resize(L0.rowPtr[nC]);
+        L0.entry.resize(L0.rowPtr[nC]);
+        L0.val.resize(L0.rowPtr[nC]);
+        L0.diagPos.assign(nC, -1);
+        std::vector<std::pair<int, int>> row;
+        for (int c = 0; c < nC; ++c) {
+            row.clear();
+            row.push_back({c, c});
+            for (int e = cfOff[c]; e < cfOff[c + 1]; ++e) {
+                int f = cfFace[e], oth = cfOther[e];
+                if (oth >= 0) row.push_back({oth, nC + f});              // upper: row own, col nbr
+                else row.push_back({-(oth + 1), nC + nIF + f});           // lower: row nbr, col own
+            }
+            std::stable_sort(row.begin(), row.end(), [](auto &a, auto &b) { return a.first < b.first; });
+            int pos = L0.rowPtr[c];
+            for (auto &pr : row) {
+                L0.colIdx[pos] = pr.first;
+                L0.entry[pos] = pr.second;
+                int id = pr.second;
+                L0.val[pos] = id < nC ? diag[id] : -coef[(id - nC) % nIF];
+                if (pr.first == c) L0.diagPos[c] = pos;
+                ++pos;
+            }
+        }
+    }
+    while ((int)lv.size() < btm::kMaxLevels && lv.back().n > btm::kCoarseDirect) {
+        HLevel &F = lv.back();
+        int nc = aggregate(F, F.map);
+        if (nc == 0 || nc >= F.n) { F.map.clear(); break; }
+        F.nCoarse = nc;
+        HLevel Cl;
+        galerkin(F, Cl);
+        lv.push_back(std::move(Cl));
+    }
+    for (auto &L : lv) colour(L);
+    const int nL = (int)lv.size();
+    D.nLevels = nL;
+    D.coarseDirect = lv.back().n <= btm::kCoarseDirect ? 1 : 0;
+    C->amgCoarseN = lv.back().n;
+
+    // ---- index validation: every gather index the kernels use is checked
+    // against the buffer it indexes before anything reaches the device ------
+    auto inRange = [](const std::vector<int> &v, int lo, int hi, const char *what) {
+        for (int x : v)
+            if (x < lo || x >= hi) throw BtmError(BTM_ERR_INTERNAL, std::string("index out of range: ") + what);
+    };
+    inRange(cfFace, 0, std::max(nIF, 1), "cfFace");
+    for (int x : cfOther)
+        if (!((x >= 0 && x < nC) || (x < 0 && -(x + 1) < nC))) throw BtmError(BTM_ERR_INTERNAL, "cfOther");
+    if (cbOff[nC] > 0) inRange(std::vector<int>(cbFace.begin(), cbFace.begin() + cbOff[nC]), 0, nB, "cbFace");
+    if (cbpOff[nC] > 0) inRange(std::vector<int>(cbpFace.begin(), cbpFace.begin() + cbpOff[nC]), 0, nB, "cbpFace");
+    inRange(pin, -1, std::max(nB, 1), "pinFace");
+    for (int l = 0; l < (int)lv.size(); ++l) {
+        const HLevel &L = lv[l];
+        inRange(L.colIdx, 0, L.n, "colIdx");
+        inRange(L.colorRows, 0, L.n, "colorRows");
+        if ((int)L.colorRows.size() != L.n) throw BtmError(BTM_ERR_INTERNAL, "colour partition");
+        if (l >= 1) {
+            const int fineSize = l == 1 ? nC + 2 * nIF : (int)lv[l - 1].colIdx.size();
+            inRange(L.gIdx, 0, fineSize, "gIdx");
+            if ((int)L.gOff.size() != (int)L.colIdx.size() + 1) throw BtmError(BTM_ERR_INTERNAL, "gOff");
+            for (int I = 0; I < L.n; ++I)
+                if (L.diagPos[I] >= (int)L.colIdx.size()) throw BtmError(BTM_ERR_INTERNAL, "diagPos");
+        }
+        if (l + 1 < (int)lv.size()) {
+            inRange(L.map, 0, lv[l + 1].n, "map");
+            inRange(L.aggMem, 0, L.n, "aggMem");
+            if ((int)L.aggOff.size() != lv[l + 1].n + 1 || L.aggOff.back() != L.n)
+                throw BtmError(BTM_ERR_INTERNAL, "aggOff");
+        }
+    }
+
+    // ---- upload ------------------------------------------------------------
+    struct Rec { size_t at; };
+    auto P = [&](auto &v) { return A.put(v); };
+    size_t o_own = P(own), o_nbr = P(nbr), o_w = P(w), o_area = P(area), o_dC = P(dC), o_nx = P(nx), o_ny = P(ny),
+           o_nz = P(nz), o_sx = P(sx), o_sy = P(sy), o_sz = P(sz), o_ex = P(ex), o_ey = P(ey), o_ez = P(ez);
+    size_t o_bown = P(bown), o_barea = P(barea), o_bdC = P(bdC), o_bdW = P(bdW), o_bnx = P(bnx), o_bny = P(bny),
+           o_bnz = P(bnz), o_bsx = P(bsx), o_bsy = P(bsy), o_bsz = P(bsz), o_bwall = P(bwall), o_bout = P(bout),
+           o_bcU = P(bcU), o_bcP = P(bcP), o_bcK = P(bcK), o_bcW = P(bcW), o_bcPp = P(bcPp), o_bvUx = P(bvUx),
+           o_bvUy = P(bvUy), o_bvUz = P(bvUz), o_bvP = P(bvP), o_bvK = P(bvK), o_bvW = P(bvW);
+    std::vector<double> vol(m->cell_volume, m->cell_volume + nC), wd(m->wall_distance, m->wall_distance + nC);
+    size_t o_vol = P(vol), o_wd = P(wd), o_cfOff = P(cfOff), o_cfFace = P(cfFace), o_cfOther = P(cfOther),
+           o_cbOff = P(cbOff), o_cbFace = P(cbFace), o_cbpOff = P(cbpOff), o_cbpFace = P(cbpFace), o_pin = P(pin);
+    struct LevOff { size_t rowPtr, colIdx, diagPos, gOff, gIdx, map, aggOff, aggMem, colorOff, colorRows; };
+    std::vector<LevOff> lo(nL);
+    int64_t valTot = 0, vecTot = 0;
+    for (int l = 0; l < nL; ++l) {
+        HLevel &L = lv[l];
+        LevOff &q = lo[l];
+        q.rowPtr = P(L.rowPtr); q.colIdx = P(L.colIdx); q.diagPos = P(L.diagPos);
+        q.gOff = P(L.gOff); q.gIdx = P(L.gIdx); q.map = P(L.map); q.aggOff = P(L.aggOff); q.aggMem = P(L.aggMem);
+        q.colorOff = P(L.colorOff); q.colorRows = P(L.colorRows);
+        btm::AmgLevelDev &dl = D.lev[l];
+        dl.n = L.n;
+        dl.nnz = l == 0 ? 0 : (int)L.colIdx.size();
+        dl.nColors = L.nColors;
+        if (l >= 1) {
+            dl.valOff = valTot; valTot += (L.colIdx.size() + 31) & ~size_t(31);
+            dl.vecOff = vecTot; vecTot += (L.n + 31) & ~31;
+        }
+    }
+    D.amgValTotal = valTot;
+    D.amgVecTotal = vecTot;
+    C->amgValTotal = valTot;
+    C->amgVecTotal = vecTot;
+    char *base = nullptr;
+    ck(cudaMalloc((void **)&base, A.off + 256), "cudaMalloc(mesh)");
+    C->meshArena = base;
+    ck(cudaMemcpy(base, A.host.data(), A.off, cudaMemcpyHostToDevice), "cudaMemcpy(mesh)");
+    auto I32 = [&](size_t at) { return (const int32_t *)(base + at); };
+    auto F64 = [&](size_t at) { return (const double *)(base + at); };
+    D.own = I32(o_own); D.nbr = I32(o_nbr); D.w = F64(o_w); D.area = F64(o_area); D.deltaC = F64(o_dC);
+    D.nx = F64(o_nx); D.ny = F64(o_ny); D.nz = F64(o_nz); D.sfx = F64(o_sx); D.sfy = F64(o_sy); D.sfz = F64(o_sz);
+    D.ex = F64(o_ex); D.ey = F64(o_ey); D.ez = F64(o_ez);
+    D.bown = I32(o_bown); D.barea = F64(o_barea); D.bdeltaC = F64(o_bdC); D.bdeltaW = F64(o_bdW);
+    D.bnx = F64(o_bnx); D.bny = F64(o_bny); D.bnz = F64(o_bnz); D.bsfx = F64(o_bsx); D.bsfy = F64(o_bsy);
+    D.bsfz = F64(o_bsz); D.bwall = I32(o_bwall); D.bout = I32(o_bout); D.bcU = I32(o_bcU); D.bcP = I32(o_bcP);
+    D.bcK = I32(o_bcK); D.bcW = I32(o_bcW); D.bcPp = I32(o_bcPp); D.bvUx = F64(o_bvUx); D.bvUy = F64(o_bvUy);
+    D.bvUz = F64(o_bvUz); D.bvP = F64(o_bvP); D.bvK = F64(o_bvK); D.bvW = F64(o_bvW);
+    D.vol = F64(o_vol); D.wd = F64(o_wd); D.cfOff = I32(o_cfOff); D.cfFace = I32(o_cfFace); D.cfOther = I32(o_cfOther);
+    D.cbOff = I32(o_cbOff); D.cbFace = I32(o_cbFace); D.cbpOff = I32(o_cbpOff); D.cbpFace = I32(o_cbpFace);
+    D.pinFace = I32(o_pin);
+    for (int l = 0; l < nL; ++l) {
+        btm::AmgLevelDev &dl = D.lev[l];
+        dl.rowPtr = I32(lo[l].rowPtr); dl.colIdx = I32(lo[l].colIdx); dl.diagPos = I32(lo[l].diagPos);
+        dl.gOff = I32(lo[l].gOff); dl.gIdx = I32(lo[l].gIdx); dl.map = I32(lo[l].map);
+        dl.aggOff = I32(lo[l].aggOff); dl.aggMem = I32(lo[l].aggMem);
+        dl.colorOff = I32(lo[l].colorOff); dl.colorRows = I32(lo[l].colorRows);
+    }
+    ck(cudaMalloc((void **)&C->dMeshPtr, sizeof(btm::DevMesh)), "cudaMalloc(DevMesh)");
+    ck(cudaMemcpy(C->dMeshPtr, &D, sizeof D, cudaMemcpyHostToDevice), "cudaMemcpy(DevMesh)");
+}
+
+// Carve one instance slab (fields + work + AMG + control words).
+void make_slab(btm_case *C, Slab &S) {
+    const int nC = C->nC, nIF = C->nIF, nB = C->nB;
+    const int nc = C->dmesh.coarseDirect ? C->amgCoarseN : 1;  // dense inverse only when small
+    const size_t al = 32;  // doubles: 256-byte alignment
+    auto up = [&](size_t n) { return (n + al - 1) & ~(al - 1); };
+    size_t cell = up(nC), face = up(std::max(nIF, 1)), bnd = up(std::max(nB, 1));
+    size_t doubles = 0;
+    doubles += 38 * cell;                     // cell arrays
+    doubles += cell + 2 * face;               // diag|upper|lower (contiguous, unpadded inside)
+    doubles += face;                          // fflux
+    doubles += 7 * bnd;                       // boundary arrays
+    doubles += up(C->amgValTotal) + 3 * up(C->amgVecTotal) + up(nC + C->amgVecTotal);
+    doubles += up((size_t)nc * nc) + up((size_t)4 * nc * nc);
+    int gridBlocks = C->maxGridBlocks > 0 ? C->maxGridBlocks : 1024;
+    doubles += up((size_t)2 * gridBlocks * btm::kRedSlots);
+    doubles += 32;                            // outLast
+    size_t bytes = doubles * 8 + 1024;        // + control words
+    char *base = nullptr;
+    ck(cudaMalloc((void **)&base, bytes), "cudaMalloc(instance)");
+    S.dptr = base;
+    S.bytes = bytes;
+    btm::DevInst &I = S.inst;
+    std::memset(&I, 0, sizeof I);
+    double *d = (double *)base;
+    auto take = [&](size_t n) { double *p = d; d += up(n); return p; };
+    double **cells[] = {&I.ux, &I.uy, &I.uz, &I.p, &I.k, &I.om, &I.nut, &I.f1, &I.f2, &I.pk, &I.cdkw, &I.smag,
+                        &I.gpx, &I.gpy, &I.gpz, &I.src, &I.aPx, &I.pp, &I.kold, &I.omold, &I.r, &I.rh,
+                        &I.pv, &I.v, &I.s, &I.t, &I.ph, &I.sh, &I.rd};
+    for (double **pp : cells) *pp = take(nC);
+    for (int q = 0; q < 9; ++q) I.g[q] = take(nC);
+    I.diag = d;
+    I.upper = d + nC;
+    I.lower = d + nC + nIF;
+    d += up((size_t)nC + 2 * (size_t)nIF);
+    I.fflux = take(std::max(nIF, 1));
+    double **bnds[] = {&I.ubx, &I.uby, &I.ubz, &I.pb, &I.kb, &I.omb, &I.ppb};
+    for (double **pp : bnds) *pp = take(std::max(nB, 1));
+    I.amgVal = take(std::max<int64_t>(C->amgValTotal, 1));
+    I.amgX = take(std::max<int64_t>(C->amgVecTotal, 1));
+    I.amgB = take(std::max<int64_t>(C->amgVecTotal, 1));
+    I.amgR = take(std::max<int64_t>(C->amgVecTotal, 1));
+    I.amgRd = take((size_t)nC + C->amgVecTotal);
+    I.ainv = take((size_t)nc * nc);
+    I.gj = take((size_t)4 * nc * nc);
+    I.gpart = take((size_t)2 * gridBlocks * btm::kRedSlots);
+    I.outLast = take(32);
+    char *ctl = (char *)d;
+    I.barrier = (unsigned int *)ctl;
+    I.err = (int32_t *)(ctl + 64);
+    I.out = (int32_t *)(ctl + 128);
+    I.outInner = (int64_t *)(ctl + 192);
+    I.outTime = (uint64_t *)(ctl + 256);
+    I.M = C->dMeshPtr;
+    if ((size_t)(ctl + 512 - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "slab overflow");
+}
+
+void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
+    I.S = dev_settings(C->settings);
+    I.nu = C->nu;
+    for (int q = 0; q < 11; ++q) I.coeff[q] = coeffs[q];
+    I.variant = variant;
+    I.initMode = init ? init->mode : 0;
+    bool zeroZ = C->is2d && C->bcZeroZ && C->settings.body_force[2] == 0.0;
+    if (I.initMode == 0) {
+        double u[3] = {1.0, 0.0, 0.0}, p = 0.0, k = 1e-4, w = 1.0;
+        if (init) { u[0] = init->u[0]; u[1] = init->u[1]; u[2] = init->u[2]; p = init->p; k = init->k; w = init->omega; }
+        I.init[0] = u[0]; I.init[1] = u[1]; I.init[2] = u[2]; I.init[3] = p; I.init[4] = k; I.init[5] = w;
+        if (u[2] != 0.0) zeroZ = false;
+        I.turbEstIn = 0;
+    } else {
+        const btm_state *ws = init->warm;
+        for (int c = 0; c < C->nC && zeroZ; ++c) if (ws->U[3 * c + 2] != 0.0) zeroZ = false;
+        for (int b = 0; b < C->nB && zeroZ; ++b) if (ws->Ub[3 * b + 2] != 0.0) zeroZ = false;
+        I.turbEstIn = ws->turb_established;
+    }
+    I.solveZ = zeroZ ? 0 : 1;
+}
+
+// host staging for SoA <-> AoS conversion
+void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
+                  std::vector<double> &stage) {
+    const int nC = C->nC, nB = C->nB;
+    stage.resize((size_t)17 * std::max(nC, nB) + 16);
+    auto send = [&](double *dst, const double *src, int n) {
+        if (n > 0) ck(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, st), "upload");
+    };
+    double *h = stage.data();
+    for (int c = 0; c < nC; ++c) { h[c] = ws->U[3 * c]; h[nC + c] = ws->U[3 * c + 1]; h[2 * nC + c] = ws->U[3 * c + 2]; }
+    send(I.ux, h, nC); send(I.uy, h + nC, nC); send(I.uz, h + 2 * nC, nC);
+    double *hb = h + 3 * nC;
+    for (int b = 0; b < nB; ++b) { hb[b] = ws->Ub[3 * b]; hb[nB + b] = ws->Ub[3 * b + 1]; hb[2 * nB + b] = ws->Ub[3 * b + 2]; }
+    send(I.ubx, hb, nB); send(I.uby, hb + nB, nB); send(I.ubz, hb + 2 * nB, nB);
+    send(I.p, ws->p, nC); send(I.pb, ws->pb, nB);
+    send(I.k, ws->k, nC); send(I.kb, ws->kb, nB);
+    send(I.om, ws->omega, nC); send(I.omb, ws->omegab, nB);
+    if (ws->nuT) send(I.nut, ws->nuT, nC);
+    if (ws->F1) send(I.f1, ws->F1, nC);
+    if (ws->F2) send(I.f2, ws->F2, nC);
+    if (ws->Pk) send(I.pk, ws->Pk, nC);
+    if (ws->CDkw) send(I.cdkw, ws->CDkw, nC);
+    ck(cudaStreamSynchronize(st), "upload sync");
+}
+
+void download_state(btm_case *C, const btm::DevInst &I, btm_state *o, cudaStream_t st, std::vector<double> &stage) {
+    const int nC = C->nC, nB = C->nB;
+    stage.resize((size_t)17 * std::max(nC, nB) + 16);
+    auto get = [&](double *dst, const double *src, int n) {
+        if (dst && n > 0) ck(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "download");
+    };
+    double *h = stage.data();
+    if (o->U) { get(h, I.ux, nC); get(h + nC, I.uy, nC); get(h + 2 * nC, I.uz, nC); }
+    double *hb = h + 3 * nC;
+    if (o->Ub) { get(hb, I.ubx, nB); get(hb + nB, I.uby, nB); get(hb + 2 * nB, I.ubz, nB); }
+    get(o->p, I.p, nC); get(o->pb, I.pb, nB); get(o->k, I.k, nC); get(o->kb, I.kb, nB);
+    get(o->omega, I.om, nC); get(o->omegab, I.omb, nB); get(o->nuT, I.nut, nC); get(o->F1, I.f1, nC);
+    get(o->F2, I.f2, nC); get(o->Pk, I.pk, nC); get(o->CDkw, I.cdkw, nC);
+    ck(cudaStreamSynchronize(st), "download sync");
+    if (o->U)
+        for (int c = 0; c < nC; ++c) { o->U[3 * c] = h[c]; o->U[3 * c + 1] = h[nC + c]; o->U[3 * c + 2] = h[2 * nC + c]; }
+    if (o->Ub)
+        for (int b = 0; b < nB; ++b) { o->Ub[3 * b] = hb[b]; o->Ub[3 * b + 1] = hb[nB + b]; o->Ub[3 * b + 2] = hb[2 * nB + b]; }
+}
+
+int block_max_cells() {
+    static int v = [] {
+        const char *e = std::getenv("BTM_BLOCK_MAX_CELLS");
+        return e ? std::atoi(e) : 16384;
+    }();
+    return v;
+}
+
+struct Job {
+    btm_case *C;
+    Slab *S;
+    int idx;
+};
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *btm_last_error(void) { return g_err.c_str(); }
+int btm_abi_version(void) { return BTM_ABI_VERSION; }
+
+int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu, const btm_settings *settings,
+                    btm_case **out) {
+    if (!mesh || !settings || !out || (mesh->n_patches > 0 && !bcs)) return fail(BTM_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (int e = ensure_device()) return e;
+    btm_case *C = new btm_case();
+    try {
+        check_settings(*settings);
+        C->nu = nu;
+        C->settings = *settings;
+        int blocks = 0;
+        if (btm::engine_grid_blocks(&blocks) != 0) throw BtmError(BTM_ERR_CUDA, "occupancy query failed");
+        C->maxGridBlocks = blocks;
+        build_case(C, mesh, bcs);
+        ck(cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    } catch (const BtmError &e) {
+        btm_case_destroy(C);
+        return fail(e.code, e.what());
+    } catch (const std::exception &e) {
+        btm_case_destroy(C);
+        return fail(BTM_ERR_INTERNAL, e.what());
+    }
+    *out = C;
+    return BTM_OK;
+}
+
+void btm_case_destroy(btm_case *C) {
+    if (!C) return;
+    for (Slab &s : C->slabs) if (s.dptr) cudaFree(s.dptr);
+    if (C->meshArena) cudaFree(C->meshArena);
+    if (C->dMeshPtr) cudaFree(C->dMeshPtr);
+    if (C->stream) cudaStreamDestroy(C->stream);
+    delete C;
+}
+
+int btm_case_info(const btm_case *C, int32_t *n_cells, int32_t *n_boundary_faces, int32_t *n_amg_levels,
+                  int32_t *is_2d) {
+    if (!C) return fail(BTM_ERR_ARG, "null case");
+    if (n_cells) *n_cells = C->nC;
+    if (n_boundary_faces) *n_boundary_faces = C->nB;
+    if (n_amg_levels) *n_amg_levels = C->dmesh.nLevels;
+    if (is_2d) *is_2d = C->is2d ? 1 : 0;
+    return BTM_OK;
+}
+
+int btm_case_set_settings(btm_case *C, const btm_settings *s) {
+    if (!C || !s) return fail(BTM_ERR_ARG, "null argument");
+    try {
+        check_settings(*s);
+    } catch (const BtmError &e) {
+        return fail(e.code, e.what());
+    }
+    bool rc = (!C->dmesh.hasOutlet || s->rhie_chow_all_meshes) ? 1 : 0;
+    if (rc != (C->dmesh.rhieChow != 0)) {
+        C->dmesh.rhieChow = rc;
+        cudaError_t e = cudaMemcpy(C->dMeshPtr, &C->dmesh, sizeof C->dmesh, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(BTM_ERR_CUDA, cudaGetErrorString(e));
+    }
+    C->settings = *s;
+    return BTM_OK;
+}
+
+int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, const int32_t *variants,
+                    const btm_init *inits, btm_state *outs, btm_history *hists) {
+    if (n < 0 || (n > 0 && (!cases || !coeffs))) return fail(BTM_ERR_ARG, "null argument");
+    if (n == 0) return BTM_OK;
+    if (int e = ensure_device()) return e;
+    try {
+        // take per-case slabs (reused across calls)
+        std::vector<Job> jobs(n);
+        std::vector<int> used;
+        std::vector<btm_case *> distinct;
+        for (int i = 0; i < n; ++i) {
+            btm_case *C = cases[i];
+            if (!C) throw BtmError(BTM_ERR_ARG, "null case in batch");
+            int slot = 0;
+            for (int j = 0; j < i; ++j) if (cases[j] == C) ++slot;
+            while ((int)C->slabs.size() <= slot) {
+                C->slabs.emplace_back();
+                make_slab(C, C->slabs.back());
+            }
+            jobs[i] = {C, nullptr, i};
+            if (std::find(distinct.begin(), distinct.end(), C) == distinct.end()) distinct.push_back(C);
+        }
+        std::vector<int> slotOf(n, 0);
+        for (int i = 0; i < n; ++i) {
+            int slot = 0;
+            for (int j = 0; j < i; ++j) if (cases[j] == cases[i]) ++slot;
+            jobs[i].S = &cases[i]->slabs[slot];
+        }
+        cudaStream_t st = cases[0]->stream;
+        std::vector<double> stage;
+        std::vector<btm::DevInst> hostInsts;
+        std::vector<int> blockIdx, gridIdx;
+        std::vector<std::vector<double>> histBufs(n);
+        std::vector<double *> histDev(n, nullptr);
+        for (int i = 0; i < n; ++i) {
+            Job &J = jobs[i];
+            btm::DevInst &I = J.S->inst;
+            const btm_init *ini = inits ? &inits[i] : nullptr;
+            fill_inst(J.C, I, coeffs + 11 * (size_t)i, variants ? variants[i] : 0, ini);
+            if (ini && ini->mode == 1) {
+                if (!ini->warm) throw BtmError(BTM_ERR_ARG, "warm init without a state");
+                upload_state(J.C, I, ini->warm, st, stage);
+            }
+            I.hist = nullptr;
+            I.histCap = 0;
+            if (hists && hists[i].residuals && hists[i].residual_capacity > 0) {
+                ck(cudaMalloc((void **)&histDev[i], sizeof(double) * 6 * hists[i].residual_capacity), "cudaMalloc(hist)");
+                I.hist = histDev[i];
+                I.histCap = hists[i].residual_capacity;
+            }
+            ck(cudaMemsetAsync(I.barrier, 0, 512, st), "memset control");
+            if (J.C->nC <= block_max_cells()) blockIdx.push_back(i);
+            else gridIdx.push_back(i);
+        }
+        // one persistent launch for all block-mode instances
+        btm::DevInst *dInsts = nullptr;
+        if (!blockIdx.empty()) {
+            std::vector<btm::DevInst> arr;
+            for (int i : blockIdx) arr.push_back(jobs[i].S->inst);
+            ck(cudaMalloc((void **)&dInsts, sizeof(btm::DevInst) * arr.size()), "cudaMalloc(insts)");
+            ck(cudaMemcpyAsync(dInsts, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
+            int e = btm::engine_launch_block(dInsts, (int)arr.size(), st);
+            if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
+        }
+        std::vector<btm::DevInst *> gridPtrs;
+        for (int i : gridIdx) {
+            btm::DevInst *dI = nullptr;
+            ck(cudaMalloc((void **)&dI, sizeof(btm::DevInst)), "cudaMalloc(inst)");
+            ck(cudaMemcpyAsync(dI, &jobs[i].S->inst, sizeof(btm::DevInst), cudaMemcpyHostToDevice, st), "inst");
+            gridPtrs.push_back(dI);
+            int e = btm::engine_launch_grid(dI, jobs[i].C->maxGridBlocks, st);
+            if (e) throw BtmError(BTM_ERR_CUDA, std::string("grid launch: ") + cudaGetErrorString((cudaError_t)e));
+        }
+        cudaError_t se = cudaStreamSynchronize(st);
+        if (dInsts) cudaFree(dInsts);
+        for (auto *p : gridPtrs) cudaFree(p);
+        if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, std::string("solve: ") + cudaGetErrorString(se));
+        for (int i = 0; i < n; ++i) {
+            Job &J = jobs[i];
+            const btm::DevInst &I = J.S->inst;
+            int32_t outv[8];
+            int64_t innerv = 0;
+            int32_t errv = 0;
+            double lastv[6];
+            ck(cudaMemcpy(outv, I.out, sizeof outv, cudaMemcpyDeviceToHost), "status");
+            ck(cudaMemcpy(&innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost), "status");
+            ck(cudaMemcpy(lastv, I.outLast, sizeof lastv, cudaMemcpyDeviceToHost), "status");
+            ck(cudaMemcpy(&errv, I.err, sizeof errv, cudaMemcpyDeviceToHost), "status");
+            uint64_t tns[8];
+            ck(cudaMemcpy(tns, I.outTime, sizeof tns, cudaMemcpyDeviceToHost), "status");
+            if (hists) {
+                btm_history &h = hists[i];
+                h.status = outv[0];
+                h.converged = outv[1];
+                h.diverged = outv[2];
+                h.final_iter = outv[3];
+                h.iterations_run = outv[4];
+                h.inner_iterations = innerv;
+                for (int q = 0; q < 6; ++q) h.last_residual[q] = lastv[q];
+                for (int q = 0; q < 8; ++q) h.phase_ms[q] = 1e-6 * (double)tns[q];
+                if (histDev[i]) {
+                    int rows = std::min(h.residual_capacity, outv[4]);
+                    ck(cudaMemcpy(h.residuals, histDev[i], sizeof(double) * 6 * rows, cudaMemcpyDeviceToHost), "hist");
+                    cudaFree(histDev[i]);
+                }
+            }
+            if (outs) {
+                download_state(J.C, I, &outs[i], st, stage);
+                outs[i].turb_established = outv[5];
+            }
+            if (errv) throw BtmError(BTM_ERR_TIMEOUT, "a bounded device wait timed out; the solve was abandoned");
+        }
+    } catch (const BtmError &e) {
+        return fail(e.code, e.what());
+    } catch (const std::exception &e) {
+        return fail(BTM_ERR_INTERNAL, e.what());
+    }
+    return BTM_OK;
+}
+
+int btm_solve(btm_case *c, const double *coeffs, int32_t variant, const btm_init *init, btm_state *out,
+              btm_history *hist) {
+    if (!c || !coeffs) return fail(BTM_ERR_ARG, "null argument");
+    btm_case *cs[1] = {c};
+    return btm_solve_batch(1, cs, coeffs, &variant, init, out, hist);
+}
+
+// Test hook: see the phase list in btm_gb300.h.  `in` packs the state
+// [U(3nC) p k omega nuT F1 F2 Pk CDkw Smag aP (nC each) Ub(3nB) pb kb omegab (nB each)]
+// followed by the linear system [diag(nC) upper(nIF) lower(nIF) source(nC) x(nC)].
+int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t variant, int32_t arg,
+                    const double *in, int64_t n_in, double *out, int64_t n_out) {
+    if (!C || !coeffs || !in || !out) return fail(BTM_ERR_ARG, "null argument");
+    const int nC = C->nC, nIF = C->nIF, nB = C->nB;
+    const int64_t need = 13LL * nC + 6LL * nB + 3LL * nC + 2LL * nIF;
+    if (n_in < need) return fail(BTM_ERR_ARG, "debug input too small");
+    if (nC > 65536) return fail(BTM_ERR_ARG, "debug phases run on one CTA: mesh too large");
+    try {
+        if (C->slabs.empty()) { C->slabs.emplace_back(); make_slab(C, C->slabs.back()); }
+        Slab &S = C->slabs[0];
+        btm::DevInst &I = S.inst;
+        btm_init ini{};
+        ini.mode = 1;
+        fill_inst(C, I, coeffs, variant, nullptr);
+        I.initMode = 1;
+        I.dbgPhase = phase;
+        I.dbgArg = arg;
+        cudaStream_t st = C->stream;
+        const double *q = in;
+        std::vector<double> U(q, q + 3 * (size_t)nC);
+        q += 3 * (size_t)nC;
+        double *cellDst[] = {I.p, I.k, I.om, I.nut, I.f1, I.f2, I.pk, I.cdkw, I.smag, I.aPx};
+        std::vector<double> ux(nC), uy(nC), uz(nC);
+        for (int c = 0; c < nC; ++c) { ux[c] = U[3 * c]; uy[c] = U[3 * c + 1]; uz[c] = U[3 * c + 2]; }
+        ck(cudaMemcpyAsync(I.ux, ux.data(), 8 * nC, cudaMemcpyHostToDevice, st), "dbg");
+        ck(cudaMemcpyAsync(I.uy, uy.data(), 8 * nC, cudaMemcpyHostToDevice, st), "dbg");
+        ck(cudaMemcpyAsync(I.uz, uz.data(), 8 * nC, cudaMemcpyHostToDevice, st), "dbg");
+        for (double *dst : cellDst) {
+            ck(cudaMemcpyAsync(dst, q, 8 * (size_t)nC, cudaMemcpyHostToDevice, st), "dbg");
+            q += nC;
+        }
+        std::vector<double> bx(nB), by(nB), bz(nB);
+        for (int b = 0; b < nB; ++b) { bx[b] = q[3 * b]; by[b] = q[3 * b + 1]; bz[b] = q[3 * b + 2]; }
+        q += 3 * (size_t)nB;
+        if (nB > 0) {
+            ck(cudaMemcpyAsync(I.ubx, bx.data(), 8 * nB, cudaMemcpyHostToDevice, st), "dbg");
+            ck(cudaMemcpyAsync(I.uby, by.data(), 8 * nB, cudaMemcpyHostToDevice, st), "dbg");
+            ck(cudaMemcpyAsync(I.ubz, bz.data(), 8 * nB, cudaMemcpyHostToDevice, st), "dbg");
+        }
+        for (double *dst : {I.pb, I.kb, I.omb}) {
+            if (nB > 0) ck(cudaMemcpyAsync(dst, q, 8 * (size_t)nB, cudaMemcpyHostToDevice, st), "dbg");
+            q += nB;
+        }
+        ck(cudaMemcpyAsync(I.diag, q, 8 * ((size_t)nC + 2 * nIF), cudaMemcpyHostToDevice, st), "dbg");
+        q += nC + 2 * (size_t)nIF;
+        ck(cudaMemcpyAsync(I.src, q, 8 * (size_t)nC, cudaMemcpyHostToDevice, st), "dbg");
+        q += nC;
+        ck(cudaMemcpyAsync(I.pp, q, 8 * (size_t)nC, cudaMemcpyHostToDevice, st), "dbg");
+        ck(cudaMemcpyAsync(I.r, q, 8 * (size_t)nC, cudaMemcpyHostToDevice, st), "dbg");
+        btm::DevInst *dI = nullptr;
+        ck(cudaMalloc((void **)&dI, sizeof I), "cudaMalloc(dbg)");
+        ck(cudaMemcpyAsync(dI, &I, sizeof I, cudaMemcpyHostToDevice, st), "dbg");
+        int e = btm::engine_launch_debug(dI, st);
+        cudaError_t se = cudaStreamSynchronize(st);
+        cudaFree(dI);
+        if (e) throw BtmError(BTM_ERR_CUDA, cudaGetErrorString((cudaError_t)e));
+        if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, cudaGetErrorString(se));
+        std::vector<const double *> srcs;
+        std::vector<int64_t> lens;
+        switch (phase) {
+            case BTM_PHASE_GRAD: srcs = {I.gpx, I.gpy, I.gpz}; lens = {nC, nC, nC}; break;
+            case BTM_PHASE_SST: srcs = {I.nut, I.f1, I.f2, I.pk, I.cdkw, I.smag}; lens.assign(6, nC); break;
+            case BTM_PHASE_MOMENTUM: srcs = {I.diag, I.src, I.aPx}; lens = {nC + 2LL * nIF, nC, nC}; break;
+            case BTM_PHASE_PRESSURE:
+            case BTM_PHASE_KEQ:
+            case BTM_PHASE_OMEGAEQ: srcs = {I.diag, I.src}; lens = {nC + 2LL * nIF, nC}; break;
+            case BTM_PHASE_SPMV: srcs = {I.v}; lens = {nC}; break;
+            case BTM_PHASE_BICGSTAB:
+            case BTM_PHASE_AMGPCG:
+            case 11: srcs = {I.pp, I.outLast}; lens = {nC, 4}; break;
+            default: throw BtmError(BTM_ERR_ARG, "unknown debug phase");
+        }
+        int64_t total = 0;
+        for (auto l : lens) total += l;
+        if (n_out < total) throw BtmError(BTM_ERR_ARG, "debug output too small");
+        double *o = out;
+        for (size_t j = 0; j < srcs.size(); ++j) {
+            ck(cudaMemcpy(o, srcs[j], 8 * (size_t)lens[j], cudaMemcpyDeviceToHost), "dbg out");
+            o += lens[j];
+        }
+    } catch (const BtmError &e) {
+        return fail(e.code, e.what());
+    } catch (const std::exception &e) {
+        return fail(BTM_ERR_INTERNAL, e.what());
+    }
+    return BTM_OK;
+}
+
+}  // extern "C"

@@ -176,6 +176,11 @@ typedef struct btm_history {
     double  last_residual[6];      /* last ResidualEntry                       */
     int32_t residual_capacity;     /* rows available in `residuals`            */
     double *residuals;             /* [residual_capacity*6] or NULL            */
+    /* device time per phase in ms, the reference's per-solve phase timers
+     * (SIMPLESolver.hpp:123-136): [0] SST closure, [1] momentum assembly,
+     * [2] momentum solves, [3] p' assembly, [4] AMG numeric setup,
+     * [5] p' solve, [6] corrections + BCs, [7] k/omega assembly+solves */
+    double  phase_ms[8];
 } btm_history;
 
 typedef struct btm_case btm_case;
@@ -193,6 +198,8 @@ int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu,
 void btm_case_destroy(btm_case *c);
 int btm_case_info(const btm_case *c, int32_t *n_cells, int32_t *n_boundary_faces,
                   int32_t *n_amg_levels, int32_t *is_2d);
+/* Replace the case's SIMPLE controls (same checks as at creation). */
+int btm_case_set_settings(btm_case *c, const btm_settings *settings);
 
 /* One forward solve on the device.  coeffs[11] are the SST constants in the
  * InferenceParameterSet order (core/include/InferenceParameters.hpp:11-14);

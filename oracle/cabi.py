@@ -58,7 +58,7 @@ class History(C.Structure):
     _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
                 ("final_iter", C.c_int32), ("iterations_run", C.c_int32),
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
-                ("residual_capacity", C.c_int32), ("residuals", _dp)]
+                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8)]
 
 
 CELL_FIELDS = ("p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw")

@@ -1,0 +1,156 @@
+"""Named test workloads shared by the golden generator and the tests.
+
+Each case is (mesh, boundary conditions, nu, settings, initial state).  Meshes
+are built by the product's factories; the golden generator stores the exact
+mesh (MSH1 bytes) next to the reference results, and the tests rebuild the
+mesh from those bytes so both sides see identical geometry on any machine.
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+PKG = os.path.join(ROOT, "bayesian-turbulence-modeling_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+from rans_sst_py import FlowBoundaryConditions, Mesh, SolverSettings, Vec3  # noqa: E402
+from rans_sst_py._types import COEFF_DEFAULTS  # noqa: E402
+
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def ratio_for_first_cell(y1: float, n_half: int, h: float = 1.0) -> float:
+    """Geometric growth ratio whose first cell of n_half cells over height h is y1."""
+    lo, hi = 1.0 + 1e-12, 3.0
+    for _ in range(200):
+        r = 0.5 * (lo + hi)
+        tot = y1 * (r ** n_half - 1.0) / (r - 1.0)
+        if tot < h:
+            lo = r
+        else:
+            hi = r
+    return 0.5 * (lo + hi)
+
+
+def channel_settings(max_iter: int, tol: float) -> SolverSettings:
+    s = SolverSettings()
+    s.verbose = False
+    s.body_force = Vec3(1.0, 0.0, 0.0)
+    s.max_iterations = max_iter
+    s.convergence_tol = tol
+    return s
+
+
+def periodic_channel(ny: int, re_tau: float, nx: int = 4, ratio: float = None, y_plus: float = 0.4):
+    """Streamwise-periodic channel at Re_tau (body force 1, nu = 1/Re_tau)."""
+    if ratio is None:
+        ratio = ratio_for_first_cell(y_plus / re_tau, ny // 2)
+    m = Mesh.make_channel_periodic_geometric(nx, ny, 1.0, 1.0, ratio)
+    m.compute_wall_distance()
+    bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    init = dict(u=(20.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
+    return m, bcs, 1.0 / re_tau, init
+
+
+def bfs_case(nxu=8, nxd=48, nyu=24, nyd=12, seed=7, nut_ratio=100.0):
+    """Backward-facing step (h=1, H=3, Lu=4, Ld=30, Re_h=36000), cells permuted
+    with numpy.random.default_rng(seed).permutation.  Inlet Tu = 1%; the inlet
+    and initial omega use nu_t/nu = 100, the reference BFS driver's start-up
+    ratio (python/case_library.py:127-129): with nu_t/nu = 10 the reference
+    solver diverges during its laminar start-up iterations."""
+    m = Mesh.make_backward_facing_step_2d(nxu, nxd, nyu, nyd, 4.0, 30.0, 1.0, 3.0, 36000.0, 1.0)
+    if seed is not None:
+        m = m.permuted(np.random.default_rng(seed).permutation(m.n_cells()))
+    m.compute_wall_distance()
+    nu = 1.0 / 36000.0
+    k_in = 1.5 * 0.01 ** 2
+    om_in = k_in / (nut_ratio * nu)
+    bcs = FlowBoundaryConditions.bfs_defaults(m, 1.0, k_in, om_in)
+    init = dict(u=(1.0, 0.0, 0.0), p=0.0, k=k_in, omega=om_in)
+    return m, bcs, nu, init
+
+
+def bfs_settings(max_iter: int, tol: float) -> SolverSettings:
+    """python/bfs_reference.py:11-31 settings with the given cap/tolerance."""
+    s = SolverSettings()
+    s.verbose = False
+    s.max_iterations = max_iter
+    s.convergence_tol = tol
+    s.divergence_limit = 1e8
+    s.alpha_u, s.alpha_p, s.alpha_k, s.alpha_omega = 0.3, 0.2, 0.4, 0.4
+    s.inner_iterations = 300
+    s.inner_tolerance = 1e-4
+    s.turb_start_iter = 30
+    s.turb_update_interval = 2
+    return s
+
+
+def couette_case(nx=4, ny=32, re_tau=500.0, u_wall=None):
+    """Streamwise-periodic plane Couette: bottom wall at rest, top wall moving."""
+    ratio = ratio_for_first_cell(0.4 / re_tau, ny // 2)
+    m = Mesh.make_channel_periodic_geometric(nx, ny, 1.0, 1.0, ratio)
+    m.compute_wall_distance()
+    if u_wall is None:
+        u_wall = 2.0 * 20.0
+    bcs = FlowBoundaryConditions.periodic_couette(m, u_wall)
+    init = dict(u=(0.5 * u_wall, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
+    return m, bcs, 1.0 / re_tau, init
+
+
+def couette_settings(max_iter, tol):
+    s = SolverSettings()
+    s.verbose = False
+    s.max_iterations = max_iter
+    s.convergence_tol = tol
+    return s
+
+
+def duct_case(nx=4, ny=16, nz=16, re_tau=150.0, ratio=1.25):
+    m = Mesh.make_square_duct_periodic_3d(nx, ny, nz, 10.0, 2.0, ratio)
+    m.compute_wall_distance()
+    bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    init = dict(u=(15.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
+    return m, bcs, 1.0 / re_tau, init
+
+
+def mesh_from_bytes(b: bytes) -> Mesh:
+    import tempfile
+    with tempfile.NamedTemporaryFile(suffix=".msh", delete=False) as fh:
+        fh.write(b)
+        path = fh.name
+    try:
+        m = Mesh.load_from_file(path)
+    finally:
+        os.unlink(path)
+    return m
+
+
+def mesh_to_bytes(m: Mesh) -> bytes:
+    import tempfile
+    with tempfile.NamedTemporaryFile(suffix=".msh", delete=False) as fh:
+        path = fh.name
+    try:
+        m.save_binary(path)
+        with open(path, "rb") as fh:
+            return fh.read()
+    finally:
+        os.unlink(path)
+
+
+def load_golden(name: str) -> dict:
+    path = os.path.join(GOLDEN, name + ".npz")
+    z = np.load(path, allow_pickle=False)
+    return {k: z[k] for k in z.files}
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

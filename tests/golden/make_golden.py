@@ -1,0 +1,216 @@
+"""Generate the golden vectors under tests/golden/ by running the UNMODIFIED
+reference solver (compiled from its own sources by `make -C oracle ref`,
+driven through oracle/ref_driver.cpp).  Run in a checkout where the
+reference sources exist:
+
+    make -C oracle ref
+    python tests/golden/make_golden.py [case ...]
+
+Each .npz holds the exact mesh (MSH1 bytes), the case inputs (nu, settings as
+JSON, initial state) and the reference outputs.  Stagnation states are the
+reference run for a fixed, large iteration count with the convergence test
+disabled (tol 0): two FP64 implementations stopped at a 1e-8 scaled residual
+can differ by ~1e-6, run to stagnation they agree to round-off.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+import cases  # noqa: E402
+from oracle import port  # noqa: E402
+from oracle import refdriver as rd  # noqa: E402
+from oracle.cabi import History  # noqa: E402
+
+COEFF = np.array(cases.COEFF_DEFAULTS)
+FIELDS = ("U", "p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw", "Ub", "pb", "kb", "omegab")
+
+
+def settings_json(s) -> np.ndarray:
+    d = {k: (v if not hasattr(v, "x") else [v.x, v.y, v.z]) for k, v in s.__dict__.items()}
+    return np.frombuffer(json.dumps(d, sort_keys=True).encode(), np.uint8)
+
+
+def ref_solve(mesh_bytes, mesh, bcs, nu, s, init, coeffs=COEFF, variant=0, residual_capacity=0):
+    path = "/tmp/_golden_mesh.msh"
+    with open(path, "wb") as fh:
+        fh.write(mesh_bytes)
+    rm = rd.RefMesh.load(path)
+    rm.wall_distance()
+    bca, keep = port.bc_array(bcs)
+    st = port.settings_struct(s)
+    ini, _ = port.make_init(**init)
+    t0 = time.time()
+    arrays, hist, res = rm.solve(bca, nu, st, coeffs, variant, ini, mesh.n_cells(), mesh.n_boundary_faces(),
+                                 residual_capacity)
+    dt = time.time() - t0
+    info = dict(final_iter=hist.final_iter, iterations_run=hist.iterations_run, converged=hist.converged,
+                diverged=hist.diverged, seconds=dt)
+    return arrays, info, res
+
+
+def pack(prefix, arrays, info, out):
+    for f in FIELDS:
+        out[f"{prefix}_{f}"] = arrays[f]
+    out[f"{prefix}_turb_established"] = np.array(arrays["turb_established"])
+    for k, v in info.items():
+        out[f"{prefix}_{k}"] = np.array(v)
+
+
+def base_record(mesh, nu, s, init):
+    mb = cases.mesh_to_bytes(mesh)
+    return mb, {"mesh": np.frombuffer(mb, np.uint8), "wall_dist": mesh.wall_dist, "nu": np.array(nu),
+                "settings": settings_json(s),
+                "init": np.array([*init["u"], init["p"], init["k"], init["omega"]])}
+
+
+def make_chan180():
+    m, bcs, nu, init = cases.periodic_channel(32, 180.0)
+    s = cases.channel_settings(20000, 0.0)
+    mb, out = base_record(m, nu, s, init)
+    for n in (1, 5, 50):
+        s.max_iterations, s.convergence_tol = n, 0.0
+        a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+        pack(f"pin{n}", a, info, out)
+    s.max_iterations, s.convergence_tol = 20000, 1e-8
+    a, info, res = ref_solve(mb, m, bcs, nu, s, init, residual_capacity=20000)
+    pack("conv", a, info, out)
+    out["conv_residuals"] = res[:info["iterations_run"]]
+    s.max_iterations, s.convergence_tol = 20000, 0.0
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("stag", a, info, out)
+    return out
+
+
+def make_c1():
+    """The plane-channel workload: 4x128, geometric ratio 1.08 from each wall,
+    Re_tau = 550 (nu = 1/550, body force 1), U0 = 20, k0 = 1e-2, omega0 = 10."""
+    m, bcs, nu, init = cases.periodic_channel(128, 550.0, ratio=1.08)
+    s = cases.channel_settings(60000, 1e-8)
+    mb, out = base_record(m, nu, s, init)
+    a, info, res = ref_solve(mb, m, bcs, nu, s, init, residual_capacity=60000)
+    pack("conv", a, info, out)
+    out["conv_residuals"] = res[:info["iterations_run"]]
+    s.max_iterations, s.convergence_tol = 60000, 0.0
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("stag", a, info, out)
+    return out
+
+
+def make_bfs():
+    m, bcs, nu, init = cases.bfs_case()
+    s = cases.bfs_settings(1, 0.0)
+    mb, out = base_record(m, nu, s, init)
+    for n in (1, 5, 40):
+        s.max_iterations = n
+        a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+        pack(f"pin{n}", a, info, out)
+    # trajectory pin with a tight pressure-correction tolerance: the GPU's
+    # pressure AMG differs from the reference's sequential one, so trajectories
+    # coincide only when both pressure solves are converged tightly
+    s.max_iterations, s.convergence_tol, s.inner_tolerance = 300, 0.0, 1e-12
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("traj300", a, info, out)
+    return out
+
+
+def make_couette():
+    m, bcs, nu, init = cases.couette_case()
+    s = cases.couette_settings(30000, 1e-8)
+    mb, out = base_record(m, nu, s, init)
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("conv", a, info, out)
+    s.max_iterations, s.convergence_tol = 30000, 0.0
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("stag", a, info, out)
+    return out
+
+
+def make_duct():
+    m, bcs, nu, init = cases.duct_case()
+    s = cases.channel_settings(1, 0.0)
+    mb, out = base_record(m, nu, s, init)
+    for n in (1, 5):
+        s.max_iterations = n
+        a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+        pack(f"pin{n}", a, info, out)
+    s.max_iterations, s.convergence_tol = int(os.environ.get("DUCT_STAG_ITERS", "15000")), 0.0
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("stag", a, info, out)
+    return out
+
+
+def make_units():
+    """Known-answer vectors for the pieces: Green-Gauss gradient, SST fields and
+    the four linear solvers on seeded random inputs (BFS mesh)."""
+    rng = np.random.default_rng(1234)
+    m, bcs, nu, init = cases.bfs_case(4, 12, 8, 4)
+    mb, out = base_record(m, nu, cases.bfs_settings(1, 0.0), init)
+    path = "/tmp/_golden_mesh.msh"
+    with open(path, "wb") as fh:
+        fh.write(mb)
+    rm = rd.RefMesh.load(path)
+    rm.wall_distance()
+    nC, nB, nIF = m.n_cells(), m.n_boundary_faces(), m.n_internal_faces()
+    phi, phib = rng.normal(size=nC), rng.normal(size=nB)
+    out["gg_phi"], out["gg_phib"], out["gg_grad"] = phi, phib, rm.green_gauss(phi, phib)
+    U, Ub = rng.normal(size=(nC, 3)) * [1, 0.3, 0], rng.normal(size=(nB, 3)) * [1, 0.3, 0]
+    k, kb = rng.uniform(1e-5, 1e-2, nC), rng.uniform(0, 1e-2, nB)
+    om, omb = rng.uniform(1, 1e4, nC), rng.uniform(1, 1e4, nB)
+    for name, v in (("U", U), ("Ub", Ub), ("k", k), ("kb", kb), ("om", om), ("omb", omb)):
+        out["sst_in_" + name] = v
+    coeffs = COEFF * rng.uniform(0.8, 1.2, 11)
+    out["sst_coeffs"] = coeffs
+    for variant in (0, 1, 2):
+        r = rm.sst_fields(coeffs, variant, nu, U, Ub, k, kb, om, omb)
+        for key, v in r.items():
+            out[f"sst{variant}_{key}"] = v
+    own, nbr = m.owner[:nIF], m.neighbour[:nIF]
+    # a diagonally dominant nonsymmetric and a symmetric (Laplacian-like) system
+    up, lo = -rng.uniform(0.1, 1.0, nIF), -rng.uniform(0.1, 1.0, nIF)
+    diag = np.zeros(nC)
+    np.add.at(diag, own, -lo)
+    np.add.at(diag, nbr, -up)
+    diag += rng.uniform(0.05, 0.5, nC)
+    src, x0 = rng.normal(size=nC), rng.normal(size=nC)
+    sym = -rng.uniform(0.1, 1.0, nIF)
+    sdiag = np.zeros(nC)
+    np.add.at(sdiag, own, -sym)
+    np.add.at(sdiag, nbr, -sym)
+    sdiag[0] *= 2.0
+    for name, v in (("diag", diag), ("upper", up), ("lower", lo), ("src", src), ("x0", x0),
+                    ("sdiag", sdiag), ("sym", sym)):
+        out["ls_" + name] = v
+    out["ls_y"] = rd.matvec(own, nbr, diag, up, lo, x0)
+    for kind in (0, 1, 2, 3):
+        if kind in (0, 3):
+            x, res = rd.linear_solve(kind, own, nbr, sdiag, sym, sym, src, np.zeros(nC), 200, 1e-6)
+        else:
+            x, res = rd.linear_solve(kind, own, nbr, diag, up, lo, src, x0, 200, 1e-6)
+        out[f"ls{kind}_x"], out[f"ls{kind}_res"] = x, res
+    return out
+
+
+MAKERS = {"units": make_units, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
+          "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1}
+
+
+def main(names):
+    if not rd.available():
+        raise SystemExit("reference driver not built: make -C oracle ref")
+    for name in names or list(MAKERS):
+        t0 = time.time()
+        out = MAKERS[name]()
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **out)
+        print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB in {time.time() - t0:.0f} s", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

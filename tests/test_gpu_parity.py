@@ -1,0 +1,306 @@
+"""GPU parity: the sm_103a engine against the oracle and the reference goldens.
+
+Tolerances (stated per test):
+  * assembly kernels, Green-Gauss gradient, CDkw, |S|: bit-exact (the engine
+    is compiled with -fmad=false and gathers face terms in the reference's
+    face order);
+  * SST blending functions (tanh): 1e-15 relative (libm vs CUDA tanh);
+  * Krylov solves: same iterations, iterates within 1e-11 relative (parallel
+    dot products round differently);
+  * converged fields run to stagnation: 1e-8 relative L2 for U, k, omega, nu_t
+    (the spec bar); pressure 1e-8 of the dynamic pressure 0.5*max|U|^2
+    (on periodic domains p is a near-constant whose level is path-dependent).
+"""
+import json
+
+import numpy as np
+import pytest
+
+import cases
+from rans_sst_py import FlowBoundaryConditions, SolverSettings, Vec3, Case, solve, solve_batch
+from rans_sst_py._lib import PHASES, check, dptr, lib
+
+pytestmark = pytest.mark.gpu
+
+COEFF = cases.COEFF_DEFAULTS
+
+
+def settings_from(g):
+    d = json.loads(bytes(g["settings"]).decode())
+    s = SolverSettings()
+    for k, v in d.items():
+        setattr(s, k, Vec3(*v) if k == "body_force" else v)
+    return s
+
+
+def init_from(g):
+    a = g["init"]
+    return dict(u=tuple(a[:3]), p=float(a[3]), k=float(a[4]), omega=float(a[5]))
+
+
+def mesh_from(g):
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    m.compute_wall_distance()
+    assert np.array_equal(m.wall_dist, g["wall_dist"])
+    return m
+
+
+# ---------------------------------------------------------------------------
+# per-phase parity through the C ABI test hook
+# ---------------------------------------------------------------------------
+def _pack(mesh, st, sysv=None):
+    nC, nIF = mesh.n_cells(), mesh.n_internal_faces()
+    parts = [st["U"].ravel()] + [st[k] for k in ("p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw", "Smag", "aP")]
+    parts += [st["Ub"].ravel(), st["pb"], st["kb"], st["omegab"]]
+    if sysv is None:
+        sysv = dict(diag=np.zeros(nC), upper=np.zeros(nIF), lower=np.zeros(nIF), source=np.zeros(nC), x=np.zeros(nC))
+    parts += [sysv["diag"], sysv["upper"], sysv["lower"], sysv["source"], sysv["x"]]
+    return np.ascontiguousarray(np.concatenate(parts))
+
+
+def _dbg(case, phase, inp, n_out, arg=0, coeffs=COEFF):
+    cf = np.array(coeffs, float)
+    out = np.zeros(n_out)
+    check(lib().btm_debug_phase(case.h, PHASES[phase], dptr(cf), 0, arg, dptr(inp), inp.size, dptr(out), n_out))
+    return out
+
+
+def _rand_state(mesh, rng, zero_z):
+    nC, nB = mesh.n_cells(), mesh.n_boundary_faces()
+    zs = 0.0 if zero_z else 0.3
+    return dict(U=rng.normal(size=(nC, 3)) * [1, 0.3, zs], Ub=rng.normal(size=(nB, 3)) * [1, 0.3, zs],
+                p=rng.normal(size=nC), pb=rng.normal(size=nB), k=rng.uniform(1e-4, 1e-2, nC),
+                kb=rng.uniform(0, 1e-2, nB), omega=rng.uniform(1, 1e3, nC), omegab=rng.uniform(1, 1e3, nB),
+                nuT=rng.uniform(0, 1e-3, nC), F1=rng.uniform(0, 1, nC), F2=rng.uniform(0, 1, nC),
+                Pk=rng.uniform(0, 1e-2, nC), CDkw=rng.normal(size=nC) * 1e-3, Smag=rng.uniform(0, 100, nC),
+                aP=rng.uniform(0.5, 2, nC), turb_established=1)
+
+
+def _phase_meshes():
+    out = []
+    m, bcs, nu, _ = cases.bfs_case(4, 12, 8, 4)
+    s = cases.bfs_settings(10, 0.0)
+    out.append(("bfs_perm", m, bcs, nu, s, True))
+    m, bcs, nu, _ = cases.periodic_channel(32, 180.0)
+    out.append(("channel", m, bcs, nu, cases.channel_settings(10, 0.0), True))
+    m, bcs, nu, _ = cases.duct_case(3, 6, 6)
+    out.append(("duct3d", m, bcs, nu, cases.channel_settings(10, 0.0), False))
+    return out
+
+
+@pytest.fixture(scope="module", params=_phase_meshes(), ids=lambda p: p[0])
+def phase_case(request):
+    name, m, bcs, nu, s, zero_z = request.param
+    return name, m, bcs, nu, s, zero_z, Case(m, bcs, nu, s)
+
+
+def test_phase_gradient_bitexact(phase_case, oracle):
+    name, m, bcs, nu, s, zz, case = phase_case
+    st = _rand_state(m, np.random.default_rng(1), zz)
+    nC = m.n_cells()
+    g = _dbg(case, "grad", _pack(m, st), 3 * nC).reshape(3, nC).T
+    assert np.array_equal(g, oracle.green_gauss(m, st["p"], st["pb"]))
+
+
+def test_phase_sst(phase_case, oracle):
+    name, m, bcs, nu, s, zz, case = phase_case
+    st = _rand_state(m, np.random.default_rng(2), zz)
+    nC = m.n_cells()
+    o = _dbg(case, "sst", _pack(m, st), 6 * nC).reshape(6, nC)
+    ref = oracle.sst_fields(m, COEFF, 0, nu, st["U"], st["Ub"], st["k"], st["kb"], st["omega"], st["omegab"])
+    for i, key in enumerate(("nuT", "F1", "F2", "Pk", "CDkw", "Smag")):
+        if key in ("CDkw", "Smag"):
+            assert np.array_equal(o[i], ref[key]), key
+        else:  # tanh in F1/F2 (and nu_t, Pk through F2): last-bit differences only
+            assert np.max(np.abs(o[i] - ref[key])) <= 1e-15 * max(np.max(np.abs(ref[key])), 1e-300), key
+
+
+@pytest.mark.parametrize("comp", [0, 1, 2])
+def test_phase_momentum_bitexact(phase_case, oracle, comp):
+    name, m, bcs, nu, s, zz, case = phase_case
+    if zz and comp == 2:
+        pytest.skip("2-D mesh")
+    st = _rand_state(m, np.random.default_rng(3 + comp), zz)
+    nC, nIF = m.n_cells(), m.n_internal_faces()
+    o = _dbg(case, "momentum", _pack(m, st), 3 * nC + 2 * nIF, arg=comp)
+    ref = oracle.assemble(m, bcs, nu, s, COEFF, comp, st)
+    assert np.array_equal(o[:nC], ref["diag"])
+    assert np.array_equal(o[nC:nC + nIF], ref["upper"])
+    assert np.array_equal(o[nC + nIF:nC + 2 * nIF], ref["lower"])
+    assert np.array_equal(o[nC + 2 * nIF:2 * nC + 2 * nIF], ref["source"])
+    if comp == 0:
+        assert np.array_equal(o[2 * nC + 2 * nIF:], ref["aP"])
+
+
+@pytest.mark.parametrize("kind,phase", [(3, "pressure"), (4, "k"), (5, "omega")])
+def test_phase_scalar_systems_bitexact(phase_case, oracle, kind, phase):
+    name, m, bcs, nu, s, zz, case = phase_case
+    st = _rand_state(m, np.random.default_rng(10 + kind), zz)
+    nC, nIF = m.n_cells(), m.n_internal_faces()
+    o = _dbg(case, phase, _pack(m, st), 2 * nC + 2 * nIF)
+    ref = oracle.assemble(m, bcs, nu, s, COEFF, kind, st, aP=st["aP"], Smag=st["Smag"])
+    assert np.array_equal(o[:nC], ref["diag"])
+    assert np.array_equal(o[nC:nC + 2 * nIF], np.concatenate([ref["upper"], ref["lower"]]))
+    assert np.array_equal(o[nC + 2 * nIF:], ref["source"])
+
+
+def test_linear_solvers(phase_case, oracle):
+    name, m, bcs, nu, s, zz, case = phase_case
+    st = _rand_state(m, np.random.default_rng(20), zz)
+    nC, nIF = m.n_cells(), m.n_internal_faces()
+    own, nbr = m.owner[:nIF], m.neighbour[:nIF]
+    mom = oracle.assemble(m, bcs, nu, s, COEFF, 0, st)
+    sysv = dict(diag=mom["diag"], upper=mom["upper"], lower=mom["lower"], source=mom["source"],
+                x=st["U"][:, 0].copy())
+    inp = _pack(m, st, sysv)
+    y = _dbg(case, "spmv", inp, nC)
+    yr = oracle.matvec(own, nbr, mom["diag"], mom["upper"], mom["lower"], sysv["x"])
+    assert np.max(np.abs(y - yr)) <= 1e-13 * np.max(np.abs(yr))
+    o = _dbg(case, "bicgstab", inp, nC + 4)
+    xr, rr = oracle.linear_solve(1, own, nbr, mom["diag"], mom["upper"], mom["lower"], mom["source"], sysv["x"],
+                                 s.inner_iterations, s.inner_tolerance)
+    assert int(o[nC]) == int(rr[0])
+    assert abs(o[nC + 2] - rr[2]) <= 1e-12 * rr[2]
+    assert np.max(np.abs(o[:nC] - xr)) <= 1e-11 * np.max(np.abs(xr))
+    # AMG-PCG on the pressure-correction system: a different (parallel) AMG
+    # than the reference's, so compare against the exact solution instead
+    pr = oracle.assemble(m, bcs, nu, s, COEFF, 3, st, aP=st["aP"])
+    sysp = dict(diag=pr["diag"], upper=pr["upper"], lower=pr["lower"], source=pr["source"], x=np.zeros(nC))
+    o = _dbg(case, "amgpcg", _pack(m, st, sysp), nC + 4)
+    assert o[nC + 3] == 1.0 and o[nC + 1] < s.inner_tolerance
+    xd, rd = oracle.linear_solve(3, own, nbr, pr["diag"], pr["upper"], pr["lower"], pr["source"], np.zeros(nC),
+                                 1000, 1e-13)
+    A = np.diag(pr["diag"])
+    A[own, nbr] += pr["upper"]
+    A[nbr, own] += pr["lower"]
+    res = np.linalg.norm(pr["source"] - A @ o[:nC]) / np.linalg.norm(pr["source"])
+    assert res < s.inner_tolerance * 1.0001
+
+
+# ---------------------------------------------------------------------------
+# converged solves against the reference goldens
+# ---------------------------------------------------------------------------
+def _assert_fields(out, g, prefix, tol):
+    for f in ("U", "k", "omega", "nuT"):
+        assert cases.rel_l2(out.state[f], g[f"{prefix}_{f}"]) <= tol, f
+    dyn = 0.5 * np.max(np.abs(g[f"{prefix}_U"])) ** 2
+    dp = out.state["p"] - g[f"{prefix}_p"]
+    assert np.max(np.abs(dp)) <= tol * dyn
+
+
+@pytest.mark.parametrize("name,bcs_fn", [
+    ("chan180_4x32", lambda m: FlowBoundaryConditions.channel_defaults(m, 0, 0, 0)),
+    ("couette_4x32", lambda m: FlowBoundaryConditions.periodic_couette(m, 40.0)),
+])
+def test_stagnation_parity(name, bcs_fn):
+    """Run to the same stagnation iteration count as the reference: 1e-8 rel L2."""
+    g = cases.load_golden(name)
+    m = mesh_from(g)
+    s = settings_from(g)
+    s.max_iterations, s.convergence_tol = int(g["stag_iterations_run"]), 0.0
+    case = Case(m, bcs_fn(m), float(g["nu"]), s)
+    out = solve(case, COEFF, 0, init_from(g))
+    assert out.iterations_run == int(g["stag_iterations_run"])
+    _assert_fields(out, g, "stag", 1e-8)
+
+
+def test_converged_parity_channel():
+    """Stopped at the 1e-8 scaled residual like the reference: the stopping
+    iteration agrees within 5% and the fields within the ~1e-6 that separates
+    a 1e-8 stop from the fixed point."""
+    g = cases.load_golden("chan180_4x32")
+    m = mesh_from(g)
+    s = settings_from(g)
+    s.max_iterations, s.convergence_tol = 40000, 1e-8
+    case = Case(m, FlowBoundaryConditions.channel_defaults(m, 0, 0, 0), float(g["nu"]), s)
+    out = solve(case, COEFF, 0, init_from(g))
+    assert out.converged
+    ref_it = int(g["conv_final_iter"])
+    assert abs(out.final_iter - ref_it) <= 0.05 * ref_it
+    for f in ("U", "k", "omega", "nuT"):
+        assert cases.rel_l2(out.state[f], g[f"stag_{f}"]) <= 1e-6
+
+
+def test_bfs_trajectory_parity():
+    """Permuted BFS (random cell ids): 300 outer iterations with the pressure
+    correction converged tightly on both sides follow the same trajectory."""
+    g = cases.load_golden("bfs_perm_1920")
+    m = mesh_from(g)
+    s = settings_from(g)
+    s.max_iterations, s.convergence_tol, s.inner_tolerance = 300, 0.0, 1e-12
+    ini = init_from(g)
+    case = Case(m, FlowBoundaryConditions.bfs_defaults(m, 1.0, ini["k"], ini["omega"]), float(g["nu"]), s)
+    out = solve(case, COEFF, 0, ini)
+    for f in ("U", "p", "k", "omega", "nuT"):
+        assert cases.rel_l2(out.state[f], g[f"traj300_{f}"]) <= 1e-8, f
+
+
+def test_duct3d_stagnation_parity():
+    g = cases.load_golden("duct_4x16x16")
+    m = mesh_from(g)
+    s = settings_from(g)
+    s.max_iterations, s.convergence_tol = int(g["stag_iterations_run"]), 0.0
+    case = Case(m, FlowBoundaryConditions.channel_defaults(m, 0, 0, 0), float(g["nu"]), s)
+    out = solve(case, COEFF, 0, init_from(g))
+    _assert_fields(out, g, "stag", 1e-8)
+
+
+# ---------------------------------------------------------------------------
+# batching, determinism, API semantics
+# ---------------------------------------------------------------------------
+def test_batch_matches_solo_bitwise():
+    """An instance gives bit-identical results alone and inside a mixed batch."""
+    m1, b1, nu1, i1 = cases.periodic_channel(32, 180.0)
+    m2, b2, nu2, i2 = cases.couette_case(4, 16)
+    c1 = Case(m1, b1, nu1, cases.channel_settings(300, 0.0))
+    c2 = Case(m2, b2, nu2, cases.couette_settings(300, 0.0))
+    th = np.array(COEFF)
+    th2 = th.copy()
+    th2[9] *= 1.1
+    solo = solve(c1, th2, 0, i1)
+    batch = solve_batch([c2, c1, c1, c2], [th, th2, th, th2], None, [i2, i1, i1, i2])
+    for f in ("U", "p", "k", "omega", "nuT", "Ub", "pb"):
+        assert np.array_equal(batch[1].state[f], solo.state[f]), f
+    assert not np.array_equal(batch[1].state["U"], batch[2].state["U"])
+
+
+def test_kappa_is_inert():
+    """kappa enters no solved equation (InferenceParameters.hpp:130-136):
+    bit-identical results when only kappa changes."""
+    m, b, nu, ini = cases.periodic_channel(32, 180.0)
+    c = Case(m, b, nu, cases.channel_settings(200, 0.0))
+    th = np.array(COEFF)
+    th2 = th.copy()
+    th2[10] = 0.45
+    o1, o2 = solve_batch([c, c], [th, th2], None, [ini, ini])
+    for f in ("U", "p", "k", "omega", "nuT"):
+        assert np.array_equal(o1.state[f], o2.state[f])
+
+
+def test_forward_model_api():
+    import rans_sst_py as rs
+    m, bcs, nu, ini = cases.periodic_channel(32, 180.0)
+    s = cases.channel_settings(6000, 1e-6)
+    obs = rs.ObservationOperator()
+    obs.add_skin_friction("bottom_wall", rs.Vec3(0.5, 0.0, 0.5), 0.006, 0.001, 16.0)
+    obs.add_velocity_profile(rs.Vec3(0.5, 1.0, 0.5), 0, 18.0, 1.0)
+    ps = rs.InferenceParameterSet.from_indices("c3", [8, 0, 1, 9, 2, 10])
+    fm = rs.ForwardModel(m, ps, obs, bcs, nu, s, rs.Vec3(*ini["u"]), 0.0, ini["k"], ini["omega"])
+    theta = ps.pack(rs.SSTCoefficients())
+    r = fm.evaluate(theta)
+    assert r.status == rs.EvaluationStatus.Converged
+    assert len(r.predictions) == 2 and np.isfinite(r.log_lik)
+    f = fm.last_fields()
+    assert set(f) == {"U", "p", "k", "omega", "nuT", "F1", "F2", "Pk"} and f["U"].shape == (m.n_cells(), 3)
+    # kappa below its 0.35 bound: InvalidParameters without a solve
+    bad = list(theta)
+    bad[5] = 0.30
+    rb = fm.evaluate(bad)
+    assert rb.status == rs.EvaluationStatus.InvalidParameters and rb.log_lik == -1e30
+    assert fm.penalized_log_likelihood(bad) == -1e30
+    # a nearby theta warm-starts from the cached converged state
+    near = list(theta)
+    near[0] *= 1.01
+    r2 = fm.evaluate(near)
+    assert r2.status in (rs.EvaluationStatus.Converged, rs.EvaluationStatus.Unconverged)
+    assert fm.cache_size() >= 1
