@@ -126,7 +126,7 @@ struct DevInst {
 
 // engine entry points (btm_engine.cu)
 int engine_block_threads();
-int engine_launch_block(DevInst *dInsts, int n, void *stream);
+int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream);
 int engine_launch_grid(DevInst *dInst, int blocks, void *stream);
 int engine_grid_blocks(int *blocks_out);
 int engine_launch_debug(DevInst *dInst, void *stream);

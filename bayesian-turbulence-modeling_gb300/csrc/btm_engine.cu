@@ -1471,7 +1471,10 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 1) k_simple_block(DevInst *insts, int n) {
+// One CTA per instance.  NT threads per CTA; small instances use NT = 256 so
+// that two instances share an SM and hide each other's latency.
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_simple_block(DevInst *insts, int n) {
     __shared__ double red[2 * 32 * kRedSlots];
     __shared__ DevMesh sM;
     __shared__ DevInst sI;
@@ -1484,6 +1487,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_simple_block(DevInst *insts, in
     BlockTeam tm{red, 0};
     simple_solve(tm, sM, sI);
 }
+template __global__ void k_simple_block<256>(DevInst *, int);
+template __global__ void k_simple_block<512>(DevInst *, int);
 
 __global__ void __launch_bounds__(kThreads, 1) k_simple_grid(DevInst *inst) {
     __shared__ double red[2 * 32 * kRedSlots];
@@ -1574,9 +1579,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_debug(DevInst *inst) {
 // ---------------------------------------------------------------------------
 int engine_block_threads() { return kThreads; }
 
-int engine_launch_block(DevInst *dInsts, int n, void *stream) {
+int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream) {
     if (n <= 0) return 0;
-    k_simple_block<<<n, kThreads, 0, (cudaStream_t)stream>>>(dInsts, n);
+    if (threads == 256)
+        k_simple_block<256><<<n, 256, 0, (cudaStream_t)stream>>>(dInsts, n);
+    else
+        k_simple_block<512><<<n, 512, 0, (cudaStream_t)stream>>>(dInsts, n);
     return (int)cudaGetLastError();
 }
 

@@ -28,6 +28,7 @@
 namespace {
 
 thread_local std::string g_err;
+thread_local double g_launch_ms = 0.0;
 
 struct BtmError : std::runtime_error {
     int code;
@@ -732,12 +733,23 @@ void download_state(btm_case *C, const btm::DevInst &I, btm_state *o, cudaStream
         for (int b = 0; b < nB; ++b) { o->Ub[3 * b] = hb[b]; o->Ub[3 * b + 1] = hb[nB + b]; o->Ub[3 * b + 2] = hb[2 * nB + b]; }
 }
 
+// Launch-shape policy (overridable for tuning): instances up to
+// BTM_BLOCK_MAX_CELLS cells run one CTA each; CTAs have 256 threads (two
+// instances per SM) when every instance in the launch has at most
+// BTM_SMALL_CELLS cells, else 512.
+int env_int(const char *name, int dflt) {
+    const char *e = std::getenv(name);
+    return e ? std::atoi(e) : dflt;
+}
 int block_max_cells() {
-    static int v = [] {
-        const char *e = std::getenv("BTM_BLOCK_MAX_CELLS");
-        return e ? std::atoi(e) : 16384;
-    }();
+    static int v = env_int("BTM_BLOCK_MAX_CELLS", 16384);
     return v;
+}
+int block_threads_for(int maxCells) {
+    static int forced = env_int("BTM_BLOCK_THREADS", 0);
+    static int small = env_int("BTM_SMALL_CELLS", 1024);
+    if (forced == 256 || forced == 512) return forced;
+    return maxCells <= small ? 256 : 512;
 }
 
 struct Job {
@@ -754,6 +766,7 @@ struct Job {
 extern "C" {
 
 const char *btm_last_error(void) { return g_err.c_str(); }
+double btm_last_launch_ms(void) { return g_launch_ms; }
 int btm_abi_version(void) { return BTM_ABI_VERSION; }
 
 int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu, const btm_settings *settings,
@@ -873,15 +886,22 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             else gridIdx.push_back(i);
         }
         // one persistent launch for all block-mode instances
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        ck(cudaEventCreate(&ev0), "event");
+        ck(cudaEventCreate(&ev1), "event");
         btm::DevInst *dInsts = nullptr;
         if (!blockIdx.empty()) {
             std::vector<btm::DevInst> arr;
             for (int i : blockIdx) arr.push_back(jobs[i].S->inst);
             ck(cudaMalloc((void **)&dInsts, sizeof(btm::DevInst) * arr.size()), "cudaMalloc(insts)");
             ck(cudaMemcpyAsync(dInsts, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
-            int e = btm::engine_launch_block(dInsts, (int)arr.size(), st);
+            int maxCells = 0;
+            for (int i : blockIdx) maxCells = std::max(maxCells, jobs[i].C->nC);
+            ck(cudaEventRecord(ev0, st), "event");
+            int e = btm::engine_launch_block(dInsts, (int)arr.size(), block_threads_for(maxCells), st);
             if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
         }
+        if (blockIdx.empty()) ck(cudaEventRecord(ev0, st), "event");
         std::vector<btm::DevInst *> gridPtrs;
         for (int i : gridIdx) {
             btm::DevInst *dI = nullptr;
@@ -891,7 +911,12 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             int e = btm::engine_launch_grid(dI, jobs[i].C->maxGridBlocks, st);
             if (e) throw BtmError(BTM_ERR_CUDA, std::string("grid launch: ") + cudaGetErrorString((cudaError_t)e));
         }
+        ck(cudaEventRecord(ev1, st), "event");
         cudaError_t se = cudaStreamSynchronize(st);
+        float ms = 0.0f;
+        if (se == cudaSuccess && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) g_launch_ms = ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
         if (dInsts) cudaFree(dInsts);
         for (auto *p : gridPtrs) cudaFree(p);
         if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, std::string("solve: ") + cudaGetErrorString(se));

@@ -97,6 +97,7 @@ def lib():
                                     C.POINTER(BtmHistory)]
             L.btm_solve_batch.argtypes = [C.c_int32, C.POINTER(C.c_void_p), _dp, _ip, C.POINTER(BtmInit),
                                           C.POINTER(BtmState), C.POINTER(BtmHistory)]
+            L.btm_last_launch_ms.restype = C.c_double
             L.btm_debug_phase.argtypes = [C.c_void_p, C.c_int32, _dp, C.c_int32, C.c_int32, _dp, C.c_int64,
                                           _dp, C.c_int64]
             _lib = L

@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark: converged RANS forward solves per second on one GB300.
+
+Workload (the batched-theta configuration on the plane-channel case):
+  * mesh: streamwise-periodic plane channel, 4 x 128 quads, geometric wall
+    stretching ratio 1.08 from each wall (64 cells per half), half-height 1,
+    Re_tau = 550 (nu = 1/550, body force 1), U0 = 20, k0 = 1e-2, omega0 = 10;
+  * 256 theta draws from numpy.random.default_rng(11).uniform(0.8, 1.2, (256, 6))
+    times the SST defaults of [beta*, sigma_k1, sigma_w1, a1, beta1, kappa];
+    draws with kappa outside [0.35, 0.5] are InvalidParameters and are served
+    without a solve, exactly as the reference's ForwardModel::evaluate does;
+  * every valid theta: a cold SIMPLE solve to the reference's 1e-8 scaled
+    residual (max 60000 outer iterations), FP64.
+One step = the whole 256-theta batch in one persistent launch.
+
+`value` is converged solves / device time of the launch (CUDA events on the
+launching stream, inputs resident).  `e2e` is the same metric through the
+public batched API (rans_sst_py.solve_batch) with host buffers: parameters
+in, every instance's full flow state copied back to the host each step.
+The working set (~110 MB of device state for 222 instances) fits in L2.
+
+`--impl reference` times the CPU restatement of the reference algorithm
+(oracle/, or the reference built from its sources when present) on all host
+cores: a bounded sample of outer iterations per process, converted to solves/s
+with the measured iterations-per-converged-solve of the GPU run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bayesian-turbulence-modeling_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+N_THETA = 256
+THETA_SEED = 11
+ACTIVE = [8, 0, 1, 9, 2, 10]
+NY, NX, RE_TAU, RATIO = 128, 4, 550.0, 1.08
+MAX_ITER, TOL = 60000, 1e-8
+INIT = dict(u=(20.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
+CPU_SAMPLE_ITERS = 1500
+WORKLOAD = "theta256_channel4x128_re550"
+
+
+def make_case_inputs():
+    import rans_sst_py as rs
+    m = rs.Mesh.make_channel_periodic_geometric(NX, NY, 1.0, 1.0, RATIO)
+    m.compute_wall_distance()
+    bcs = rs.FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    s = rs.SolverSettings()
+    s.verbose = False
+    s.body_force = rs.Vec3(1.0, 0.0, 0.0)
+    s.max_iterations = MAX_ITER
+    s.convergence_tol = TOL
+    return m, bcs, 1.0 / RE_TAU, s
+
+
+def theta_set():
+    import rans_sst_py as rs
+    ps = rs.InferenceParameterSet.from_indices("c3", ACTIVE)
+    base = np.array(ps.pack(rs.SSTCoefficients()))
+    draws = np.random.default_rng(THETA_SEED).uniform(0.8, 1.2, (N_THETA, len(ACTIVE))) * base
+    valid = [bool(ps.in_bounds(list(t))) for t in draws]
+    coeffs = np.array([ps.unpack(list(t)).to_vector() for t in draws])
+    return draws, coeffs, np.array(valid)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- algorithmic bytes (FP64, 2-D quads) -----------------------------------
+# Compulsory traffic per cell: one outer iteration's assembly, gradients, SST
+# closure, corrections and BCs (~1100 B) plus one Krylov/AMG inner iteration
+# (~376 B: two LDU mat-vecs and 29 vector streams, the BiCGStab figure).
+BYTES_PER_CELL_OUTER = 1100.0
+BYTES_PER_CELL_INNER = 376.0
+
+
+def algorithmic_bytes(n_cells, outer, inner):
+    return n_cells * (BYTES_PER_CELL_OUTER * outer + BYTES_PER_CELL_INNER * inner)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+# ---- CPU side (oracle restatement on all host cores) -----------------------
+def _cpu_worker(args):
+    idx, n_iter = args
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, PKG)
+    from oracle import port
+    m, bcs, nu, s = make_case_inputs()
+    _, coeffs, valid = theta_set()
+    s.max_iterations, s.convergence_tol = n_iter, 0.0
+    ids = np.nonzero(valid)[0]
+    c = coeffs[ids[idx % len(ids)]]
+    t0 = time.perf_counter()
+    _, h = port.solve(m, bcs, nu, s, c, 0, **INIT)
+    return h["iterations_run"], time.perf_counter() - t0
+
+
+def cpu_sample(n_proc: int, n_iter: int):
+    """Iterations/s of the CPU restatement, n_proc independent processes."""
+    from oracle import port
+    port.build()
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(n_proc) as pool:
+        res = pool.map(_cpu_worker, [(i, n_iter) for i in range(n_proc)])
+    wall = time.perf_counter() - t0
+    iters = sum(r[0] for r in res)
+    per_proc_rate = statistics.mean(r[0] / r[1] for r in res)
+    return iters / wall, per_proc_rate, wall
+
+
+def reference_kind():
+    return "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libref_driver.so")) else "port"
+
+
+# ---- distributed helpers -----------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(world, x):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    n_proc = os.cpu_count() or 1
+    _, _, valid = theta_set()
+    iters_per_solve = args.iters_per_solve
+    values = []
+    for step in range(args.warmup + args.steps):
+        it_rate, per_proc, wall = cpu_sample(n_proc, CPU_SAMPLE_ITERS)
+        if step >= args.warmup:
+            values.append(it_rate / iters_per_solve)
+    value = statistics.mean(values)
+    line = {"metric": "converged RANS solves/sec", "value": value, "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * N_THETA / max(value, 1e-30),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "n_theta": N_THETA, "n_valid": int(valid.sum()), "cells": NX * NY,
+                       "tol": TOL, "iters_per_converged_solve": iters_per_solve},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": n_proc, "kind": reference_kind(),
+                             "sample": f"{n_proc} processes x {CPU_SAMPLE_ITERS} outer iterations of the 4x128 "
+                                       f"channel per step, converted with {iters_per_solve} iterations per "
+                                       f"converged solve (extrapolated)"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import rans_sst_py as rs
+    from rans_sst_py._lib import lib
+
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    m, bcs, nu, s = make_case_inputs()
+    draws, coeffs, valid = theta_set()
+    case = rs.Case(m, bcs, nu, s)
+    ids = np.nonzero(valid)[0]
+    n = len(ids)
+    cases = [case] * n
+    cf = coeffs[ids]
+    inits = [INIT] * n
+
+    # One step = one call of the public batched API with host buffers: the
+    # parameters go in, every instance's full flow state comes back.  The
+    # device time of the persistent launch inside the call (CUDA events on
+    # its stream) gives `value`; the wall time of the whole call gives `e2e`.
+    def step():
+        t0 = time.perf_counter()
+        outs = rs.solve_batch(cases, cf, None, inits, want_state=True)
+        return outs, lib().btm_last_launch_ms(), time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    dist_barrier(world)
+    dev_ms, wall_s, conv_counts, outer, inner = [], [], [], 0, 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            outs, ms, wall = step()
+            dev_ms.append(ms)
+            wall_s.append(wall)
+            conv_counts.append(sum(o.converged for o in outs))
+            outer += sum(o.iterations_run for o in outs)
+            inner += sum(o.inner_iterations for o in outs)
+    dist_barrier(world)
+    clk = clocks.summary()
+    step_s = dist_max(world, statistics.mean(dev_ms) / 1e3)
+    converged = statistics.mean(conv_counts)
+    value = world * converged / step_s
+    e2e_s = dist_max(world, statistics.mean(wall_s))
+    e2e_value = world * converged / e2e_s
+    h2d = n * (11 * 8 + 4 + 48)
+    nb = m.n_boundary_faces()
+    d2h = n * 8 * (m.n_cells() * 11 + nb * 6)
+
+    iters_per_solve = outer / max(1, args.steps * n)
+    bytes_per_launch = algorithmic_bytes(m.n_cells(), outer / args.steps, inner / args.steps)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_per_launch / step_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": args.traffic, "peak_kind": peak_kind,
+                "note": "algorithmic bytes of the persistent solve kernel; the working set is L2-resident and "
+                        "the kernel is bound by the FP64 pipe (GB300 FP64 is 1/64 of FP32)"}
+    line = {"metric": "converged RANS solves/sec", "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_theta": N_THETA, "n_valid": int(n), "cells": m.n_cells(),
+                       "tol": TOL, "converged_per_step": converged, "iters_per_converged_solve": iters_per_solve,
+                       "inner_iters_per_outer": inner / max(1, outer), "l2": "working set L2-resident; "
+                       "no flush needed for a single persistent launch per step"},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps, "clocks": clk, "roofline": roofline}
+    if rank == 0 and not args.no_cpu_baseline:
+        n_proc = os.cpu_count() or 1
+        it_rate, _, wall_cpu = cpu_sample(n_proc, CPU_SAMPLE_ITERS)
+        line["cpu_baseline"] = {"value": it_rate / iters_per_solve, "unit": "solves/s", "cores": n_proc,
+                                "kind": reference_kind(),
+                                "sample": f"{n_proc} processes x {CPU_SAMPLE_ITERS} outer iterations of the "
+                                          f"4x128 channel ({wall_cpu:.1f} s wall), converted with the GPU run's "
+                                          f"{iters_per_solve:.0f} iterations per converged solve (extrapolated)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_profile_case():
+    """A bounded launch of the same kernel for profilers: 304 instances of the
+    4x128 channel (two per SM), 200 outer iterations each."""
+    import rans_sst_py as rs
+    from rans_sst_py._lib import lib
+    m, bcs, nu, s = make_case_inputs()
+    s.max_iterations, s.convergence_tol = 200, 0.0
+    case = rs.Case(m, bcs, nu, s)
+    _, coeffs, valid = theta_set()
+    cf = coeffs[np.nonzero(valid)[0]]
+    cf = np.concatenate([cf, cf])[:304]
+    outs = rs.solve_batch([case] * len(cf), cf, None, [INIT] * len(cf), want_state=False)
+    it = sum(o.iterations_run for o in outs)
+    inner = sum(o.inner_iterations for o in outs)
+    ms = lib().btm_last_launch_ms()
+    print(json.dumps({"profile_case": True, "instances": len(cf), "outer_iterations": it, "inner_iterations": inner,
+                      "launch_ms": ms, "bytes_algorithmic": algorithmic_bytes(m.n_cells(), it, inner)}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch, if measured")
+    ap.add_argument("--iters-per-solve", type=float, default=30681.0,
+                    help="reference arm: outer iterations per converged solve of the 4x128 channel")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one launch of 304 instances capped at 200 outer iterations (for ncu captures)")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.profile_case:
+        run_profile_case()
+        return
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -214,6 +214,11 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs,
                     const int32_t *variants, const btm_init *inits,
                     btm_state *outs, btm_history *hists);
 
+/* Device time of the kernel launches made by the most recent solve call on
+ * this thread, measured with CUDA events on the launching stream (ms); a
+ * profiling hook with no reference counterpart. */
+double btm_last_launch_ms(void);
+
 /* ---- test hooks (no reference counterpart): run one phase of the engine
  * on the device for parity tests against the oracle.  Inputs/outputs are host
  * arrays sized as documented per phase in the engine source. ---------------- */

@@ -111,12 +111,11 @@ def make_bfs():
         s.max_iterations = n
         a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
         pack(f"pin{n}", a, info, out)
-    # trajectory pin with a tight pressure-correction tolerance: the GPU's
-    # pressure AMG differs from the reference's sequential one, so trajectories
-    # coincide only when both pressure solves are converged tightly
-    s.max_iterations, s.convergence_tol, s.inner_tolerance = 300, 0.0, 1e-12
-    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
-    pack("traj300", a, info, out)
+    # converged state: the reference settings to the 1e-8 scaled residual
+    s.max_iterations, s.convergence_tol = int(os.environ.get("BFS_CONV_ITERS", "150000")), 1e-8
+    a, info, res = ref_solve(mb, m, bcs, nu, s, init, residual_capacity=s.max_iterations)
+    pack("conv", a, info, out)
+    out["conv_residuals"] = res[:info["iterations_run"]:100]
     return out
 
 
