@@ -9,6 +9,7 @@
 // colouring).  Solves reuse per-case instance slabs; each solve is one
 // persistent launch (btm_engine.cu).
 #include "btm_common.h"
+#include "btm_host_internal.h"
 
 #include "../../include/btm_gb300.h"
 
@@ -228,33 +229,7 @@ void colour(HLevel &L) {
     for (int i = 0; i < n; ++i) L.colorRows[cur[col[i]]++] = i;
 }
 
-// ---------------------------------------------------------------------------
-// case and instance objects
-// ---------------------------------------------------------------------------
-struct Slab {
-    void *dptr = nullptr;
-    size_t bytes = 0;
-    btm::DevInst inst{};   // host copy with device pointers
-};
-
 }  // namespace
-
-struct btm_case {
-    int nC = 0, nIF = 0, nB = 0, nF = 0, nP = 0;
-    double nu = 0.0;
-    btm_settings settings{};
-    bool is2d = false, bcZeroZ = true;
-    int maxGridBlocks = 0;
-    // device
-    void *meshArena = nullptr;
-    btm::DevMesh dmesh{};            // host copy with device pointers
-    btm::DevMesh *dMeshPtr = nullptr;
-    int amgCoarseN = 0;
-    int64_t amgValTotal = 0, amgVecTotal = 0;
-    std::vector<Slab> slabs;
-    std::mutex mtx;
-    cudaStream_t stream = nullptr;
-};
 
 namespace {
 
@@ -1062,3 +1037,14 @@ int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t va
 }
 
 }  // extern "C"
+
+// ---- helpers shared with btm_noalloc.cu ----------------------------------
+namespace btm_host {
+int ensure_device() { return ::ensure_device(); }
+void set_error(const std::string &msg) { g_err = msg; }
+void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
+    ::fill_inst(C, I, coeffs, variant, init);
+}
+int block_max_cells() { return ::block_max_cells(); }
+int block_threads_for(int maxCells) { return ::block_threads_for(maxCells); }
+}  // namespace btm_host

@@ -1,0 +1,47 @@
+// btm_host_internal.h - the case object behind the opaque btm_case handle and
+// the host helpers shared by btm_host.cpp and btm_noalloc.cu (internal; not
+// part of the C ABI).
+#pragma once
+#include "btm_common.h"
+
+#include "../../include/btm_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+// One per-instance slab of device scratch and its host-side descriptor.
+struct Slab {
+    void *dptr = nullptr;
+    size_t bytes = 0;
+    btm::DevInst inst{};   // host copy with device pointers
+};
+
+struct btm_case {
+    int nC = 0, nIF = 0, nB = 0, nF = 0, nP = 0;
+    double nu = 0.0;
+    btm_settings settings{};
+    bool is2d = false, bcZeroZ = true;
+    int maxGridBlocks = 0;
+    // device
+    void *meshArena = nullptr;
+    btm::DevMesh dmesh{};            // host copy with device pointers
+    btm::DevMesh *dMeshPtr = nullptr;
+    int amgCoarseN = 0;
+    int64_t amgValTotal = 0, amgVecTotal = 0;
+    std::vector<Slab> slabs;
+    std::mutex mtx;
+    cudaStream_t stream = nullptr;
+};
+
+namespace btm_host {
+int ensure_device();
+void set_error(const std::string &msg);
+// DevInst fields that do not depend on where the scratch lives (settings,
+// coefficients, initial-state mode, z-momentum switch)
+void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init);
+int block_max_cells();
+int block_threads_for(int maxCells);
+}  // namespace btm_host

@@ -23,8 +23,8 @@ BUILD = os.path.join(PKG_ROOT, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 LIB_NAME = "libbtm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["btm_engine.cu", "btm_host.cpp"]
-HEADERS = ["btm_common.h"]
+SOURCES = ["btm_engine.cu", "btm_host.cpp", "btm_noalloc.cu"]
+HEADERS = ["btm_common.h", "btm_host_internal.h"]
 
 
 def nvcc() -> str:
@@ -66,6 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                          os.path.join(BUILD, "btm_engine.o")],
         [cc] + common + ["-x", "cu", "-c", os.path.join(CSRC, "btm_host.cpp"), "-o",
                          os.path.join(BUILD, "btm_host.o")],
+        [cc] + common + ["-c", os.path.join(CSRC, "btm_noalloc.cu"), "-o", os.path.join(BUILD, "btm_noalloc.o")],
     ]
 
     def run(cmd):
@@ -75,11 +76,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose:
             print(r.stdout + r.stderr)
 
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(run, jobs))
     tmp = out + ".tmp"
     run([cc] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "btm_engine.o"),
-                       os.path.join(BUILD, "btm_host.o"), "-cudart", "static"])
+                       os.path.join(BUILD, "btm_host.o"), os.path.join(BUILD, "btm_noalloc.o"),
+                       "-cudart", "static"])
     os.replace(tmp, out)
     with open(stamp_file, "w") as fh:
         fh.write(stamp)

@@ -95,6 +95,8 @@ def lib():
             L.btm_case_set_settings.argtypes = [C.c_void_p, C.POINTER(BtmSettings)]
             L.btm_solve.argtypes = [C.c_void_p, _dp, C.c_int32, C.POINTER(BtmInit), C.POINTER(BtmState),
                                     C.POINTER(BtmHistory)]
+            L.btm_solve_noalloc.argtypes = [C.c_void_p, _dp, C.c_int32, C.POINTER(BtmInit), C.POINTER(BtmState),
+                                            C.POINTER(BtmHistory)]
             L.btm_solve_batch.argtypes = [C.c_int32, C.POINTER(C.c_void_p), _dp, _ip, C.POINTER(BtmInit),
                                           C.POINTER(BtmState), C.POINTER(BtmHistory)]
             L.btm_last_launch_ms.restype = C.c_double

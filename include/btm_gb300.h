@@ -207,6 +207,24 @@ int btm_case_set_settings(btm_case *c, const btm_settings *settings);
 int btm_solve(btm_case *c, const double *coeffs, int32_t variant,
               const btm_init *init, btm_state *out, btm_history *hist);
 
+/* btm_solve without any device allocation.  No counterpart in the reference.
+ * For callers that cannot allocate device memory while they serve requests:
+ * programs whose device memory is all owned by their own pool or budget (an
+ * extra cudaMalloc from a library would break their accounting), and
+ * latency-critical loops that cannot afford cudaMalloc/cudaFree per request
+ * (they can synchronise the device).  Such callers create their cases once at
+ * start-up and then solve here.  Same kernel, same results as btm_solve.
+ * The per-solve scratch lives in one static device array of 16 MiB per GPU,
+ * held from library load until process exit.  Meshes above 16384 cells (the
+ * one-CTA limit) and solves whose scratch plus requested residual history
+ * would exceed 16 MiB are rejected with BTM_ERR_ARG and a message.  The first call on each device looks up
+ * the array's address with that device current: make it before any stream
+ * capture.  Every call reuses the array (each call clears what must start at
+ * zero); calls are serialised within a process, and calls from two processes
+ * on one GPU at the same time would race. */
+int btm_solve_noalloc(btm_case *c, const double *coeffs, int32_t variant,
+                      const btm_init *init, btm_state *out, btm_history *hist);
+
 /* n independent solves in one persistent launch (one CTA per instance when the
  * mesh is small enough).  cases[i] may repeat.  coeffs is n*11, variants n,
  * inits n; outs/hists may be NULL or arrays of n. */
