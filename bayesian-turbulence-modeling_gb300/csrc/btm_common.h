@@ -34,6 +34,14 @@ struct AmgLevelDev {
     int64_t vecOff;       // offset of this level's x/b/r in DevInst::amgX/amgB/amgR (levels >= 1)
 };
 
+// FP32 copies of the geometry for the mixed-precision engine (reciprocals
+// precomputed in FP64, then rounded)
+struct DevGeom32 {
+    const float *w, *area, *rdelta, *nx, *ny, *nz, *ex, *ey, *ez;   // [nIF]; rdelta = 1 / deltaC
+    const float *barea, *brdelta, *bnx, *bny, *bnz;                 // [nB]; brdelta = 1 / bdeltaC
+    const float *vol, *rvol, *wd;                                   // [nC]; rvol = 1/V (1 if V <= 1e-30)
+};
+
 struct DevMesh {
     int32_t nC, nIF, nB, nF;
     int32_t is2d;          // all normals z == 0: the z-momentum system is identically zero
@@ -69,6 +77,7 @@ struct DevMesh {
     int32_t coarseDirect;      // coarsest level solved by its dense inverse
     AmgLevelDev lev[kMaxLevels];
     int64_t amgValTotal, amgVecTotal;
+    DevGeom32 g32;
 };
 
 // Scalar controls of one solve (SolverSettings fields read by the loop).
@@ -78,6 +87,25 @@ struct DevSettings {
     double convTol, divLimit, alphaU, alphaP, alphaK, alphaW, innerTol;
     double bodyForce[3];
     double kMin, kMax, omegaMin, vonKarman;
+};
+
+// FP32 bulk of one mixed-precision instance: closure fields, gradients, the
+// correction systems, Krylov and AMG work.  The flow state itself (U, p, k,
+// omega and their boundary values) stays in the FP64 arrays of DevInst.
+struct DevWork32 {
+    float *nut, *f1, *f2, *pk, *cdkw, *smag;
+    float *g[9];           // velocity gradients dU_i/dx_j at g[3*i+j]
+    float *gp[3];          // pressure gradient
+    float *diag, *upper, *lower;   // contiguous diag [nC] | upper [nIF] | lower [nIF]
+    float *src;            // right-hand side of the correction system
+    float *aPx;            // relaxed x-momentum diagonal (pressure-correction coefficient)
+    float *pp, *ppb;       // pressure correction and its boundary values
+    float *tflux;          // [nIF] transpose-stress face flux
+    float *dcoef;          // [nIF] diffusion coefficient D_f of the equation being assembled
+    float *r, *rh, *pv, *v, *s, *t, *ph, *sh, *rd, *x;
+    float *amgVal, *amgX, *amgB, *amgR, *amgRd, *ainv, *gj;
+    double *mflux;         // [nIF] FP64 face mass flux (convective defect, continuity defect)
+    double *src64;         // [nC] FP64 pressure-correction right-hand side (refinement)
 };
 
 struct DevInst {
@@ -113,8 +141,8 @@ struct DevInst {
     int32_t *err;           // error flag (nonzero: abort)
     // outputs
     int32_t *out;           // [8]: status, converged, diverged, finalIter, itersRun, turbEst, _, _
-    int64_t *outInner;      // [1] total inner iterations
-    uint64_t *outTime;      // [8] ns per phase (leader thread's globaltimer)
+    int64_t *outInner;      // [5] inner iterations: total, momentum, pressure, turbulence, refinement
+    uint64_t *outTime;      // [10] ns per phase [0..7] (leader thread's globaltimer), solve start [8] and end [9]
     double *outLast;        // [6] last residual entry
     double *hist;           // [histCap*6] or null
     int32_t histCap;
@@ -122,6 +150,8 @@ struct DevInst {
     // debug phase I/O (test hooks)
     int32_t dbgPhase, dbgArg;
     double *dbgIn, *dbgOut;
+    // mixed-precision bulk (null for the FP64 engine)
+    DevWork32 f;
 };
 
 // engine entry points (btm_engine.cu)
@@ -130,5 +160,8 @@ int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream);
 int engine_launch_grid(DevInst *dInst, int blocks, void *stream);
 int engine_grid_blocks(int *blocks_out);
 int engine_launch_debug(DevInst *dInst, void *stream);
+
+// mixed-precision engine entry points (btm_mixed.cu)
+int mixed_launch_block(DevInst *dInsts, int n, int threads, void *stream);
 
 }  // namespace btm

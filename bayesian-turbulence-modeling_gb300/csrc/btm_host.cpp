@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -285,6 +286,8 @@ void check_settings(const btm_settings &s) {
     }
     if (!(s.alpha_u > 0) || !(s.alpha_k > 0) || !(s.alpha_omega > 0))
         throw BtmError(BTM_ERR_ARG, "relaxation factors must be positive");
+    if (s.precision != BTM_PREC_FP64 && s.precision != BTM_PREC_MIXED)
+        throw BtmError(BTM_ERR_ARG, "unknown precision code");
 }
 
 void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
@@ -524,7 +527,7 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
 
     // ---- upload ------------------------------------------------------------
     struct Rec { size_t at; };
-    auto P = [&](auto &v) { return A.put(v); };
+    auto P = [&](const auto &v) { return A.put(v); };
     size_t o_own = P(own), o_nbr = P(nbr), o_w = P(w), o_area = P(area), o_dC = P(dC), o_nx = P(nx), o_ny = P(ny),
            o_nz = P(nz), o_sx = P(sx), o_sy = P(sy), o_sz = P(sz), o_ex = P(ex), o_ey = P(ey), o_ez = P(ez);
     size_t o_bown = P(bown), o_barea = P(barea), o_bdC = P(bdC), o_bdW = P(bdW), o_bnx = P(bnx), o_bny = P(bny),
@@ -534,6 +537,19 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
     std::vector<double> vol(m->cell_volume, m->cell_volume + nC), wd(m->wall_distance, m->wall_distance + nC);
     size_t o_vol = P(vol), o_wd = P(wd), o_cfOff = P(cfOff), o_cfFace = P(cfFace), o_cfOther = P(cfOther),
            o_cbOff = P(cbOff), o_cbFace = P(cbFace), o_cbpOff = P(cbpOff), o_cbpFace = P(cbpFace), o_pin = P(pin);
+    // FP32 geometry for the mixed-precision engine; reciprocals are formed in
+    // FP64 and rounded once
+    auto f32 = [](const std::vector<double> &v) { return std::vector<float>(v.begin(), v.end()); };
+    auto recip32 = [](const std::vector<double> &v, double guard, double dflt) {
+        std::vector<float> r(v.size());
+        for (size_t i = 0; i < v.size(); ++i) r[i] = (float)(v[i] > guard ? 1.0 / v[i] : dflt);
+        return r;
+    };
+    const size_t g_w = P(f32(w)), g_area = P(f32(area)), g_rdel = P(recip32(dC, 0.0, 0.0)), g_nx = P(f32(nx)),
+                 g_ny = P(f32(ny)), g_nz = P(f32(nz)), g_ex = P(f32(ex)), g_ey = P(f32(ey)), g_ez = P(f32(ez)),
+                 g_barea = P(f32(barea)), g_brdel = P(recip32(bdC, 0.0, 0.0)), g_bnx = P(f32(bnx)),
+                 g_bny = P(f32(bny)), g_bnz = P(f32(bnz)), g_vol = P(f32(vol)), g_rvol = P(recip32(vol, 1e-30, 1.0)),
+                 g_wd = P(f32(wd));
     struct LevOff { size_t rowPtr, colIdx, diagPos, gOff, gIdx, map, aggOff, aggMem, colorOff, colorRows; };
     std::vector<LevOff> lo(nL);
     int64_t valTot = 0, vecTot = 0;
@@ -573,6 +589,12 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
     D.vol = F64(o_vol); D.wd = F64(o_wd); D.cfOff = I32(o_cfOff); D.cfFace = I32(o_cfFace); D.cfOther = I32(o_cfOther);
     D.cbOff = I32(o_cbOff); D.cbFace = I32(o_cbFace); D.cbpOff = I32(o_cbpOff); D.cbpFace = I32(o_cbpFace);
     D.pinFace = I32(o_pin);
+    auto F32 = [&](size_t at) { return (const float *)(base + at); };
+    btm::DevGeom32 &G = D.g32;
+    G.w = F32(g_w); G.area = F32(g_area); G.rdelta = F32(g_rdel); G.nx = F32(g_nx); G.ny = F32(g_ny);
+    G.nz = F32(g_nz); G.ex = F32(g_ex); G.ey = F32(g_ey); G.ez = F32(g_ez); G.barea = F32(g_barea);
+    G.brdelta = F32(g_brdel); G.bnx = F32(g_bnx); G.bny = F32(g_bny); G.bnz = F32(g_bnz); G.vol = F32(g_vol);
+    G.rvol = F32(g_rvol); G.wd = F32(g_wd);
     for (int l = 0; l < nL; ++l) {
         btm::AmgLevelDev &dl = D.lev[l];
         dl.rowPtr = I32(lo[l].rowPtr); dl.colIdx = I32(lo[l].colIdx); dl.diagPos = I32(lo[l].diagPos);
@@ -639,6 +661,53 @@ void make_slab(btm_case *C, Slab &S) {
     I.outTime = (uint64_t *)(ctl + 256);
     I.M = C->dMeshPtr;
     if ((size_t)(ctl + 512 - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "slab overflow");
+}
+
+// FP32 bulk of a slab for the mixed-precision engine, allocated on the first
+// mixed solve that uses the slab.
+void ensure_mixed(btm_case *C, Slab &S) {
+    if (S.dptr32) return;
+    const int nC = C->nC, nIF = C->nIF, nB = C->nB;
+    const int nc = C->dmesh.coarseDirect ? C->amgCoarseN : 1;
+    const size_t al = 64;  // floats: 256-byte alignment
+    auto up = [&](size_t n) { return (n + al - 1) & ~(al - 1); };
+    const size_t cell = up(nC), face = up(std::max(nIF, 1)), bnd = up(std::max(nB, 1));
+    size_t floats = 0;
+    floats += 32 * cell;                      // cell arrays
+    floats += up((size_t)nC + 2 * (size_t)nIF) + 2 * face + bnd;
+    floats += up(std::max<int64_t>(C->amgValTotal, 1)) + 3 * up(std::max<int64_t>(C->amgVecTotal, 1)) +
+              up((size_t)nC + C->amgVecTotal) + up((size_t)nc * nc) + up((size_t)4 * nc * nc);
+    floats += 2 * face + 2 * cell;            // FP64 mass flux [nIF] and right-hand side [nC]
+    const size_t bytes = floats * 4 + 512;
+    char *base = nullptr;
+    ck(cudaMalloc((void **)&base, bytes), "cudaMalloc(instance fp32)");
+    S.dptr32 = base;
+    S.bytes32 = bytes;
+    btm::DevWork32 &F = S.inst.f;
+    float *d = (float *)base;
+    auto take = [&](size_t n) { float *p = d; d += up(n); return p; };
+    float **cells[] = {&F.nut, &F.f1, &F.f2, &F.pk, &F.cdkw, &F.smag, &F.src, &F.aPx, &F.pp, &F.r, &F.rh,
+                       &F.pv, &F.v, &F.s, &F.t, &F.ph, &F.sh, &F.rd, &F.x};
+    for (float **pp : cells) *pp = take(nC);
+    for (int q = 0; q < 9; ++q) F.g[q] = take(nC);
+    for (int q = 0; q < 3; ++q) F.gp[q] = take(nC);
+    F.diag = d;
+    F.upper = d + nC;
+    F.lower = d + nC + nIF;
+    d += up((size_t)nC + 2 * (size_t)nIF);
+    F.tflux = take(std::max(nIF, 1));
+    F.dcoef = take(std::max(nIF, 1));
+    F.ppb = take(std::max(nB, 1));
+    F.amgVal = take(std::max<int64_t>(C->amgValTotal, 1));
+    F.amgX = take(std::max<int64_t>(C->amgVecTotal, 1));
+    F.amgB = take(std::max<int64_t>(C->amgVecTotal, 1));
+    F.amgR = take(std::max<int64_t>(C->amgVecTotal, 1));
+    F.amgRd = take((size_t)nC + C->amgVecTotal);
+    F.ainv = take((size_t)nc * nc);
+    F.gj = take((size_t)4 * nc * nc);
+    F.mflux = (double *)take(2 * (size_t)std::max(nIF, 1));
+    F.src64 = (double *)take(2 * (size_t)nC);
+    if ((size_t)((char *)d - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "fp32 slab overflow");
 }
 
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
@@ -772,7 +841,10 @@ int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu, co
 
 void btm_case_destroy(btm_case *C) {
     if (!C) return;
-    for (Slab &s : C->slabs) if (s.dptr) cudaFree(s.dptr);
+    for (Slab &s : C->slabs) {
+        if (s.dptr) cudaFree(s.dptr);
+        if (s.dptr32) cudaFree(s.dptr32);
+    }
     if (C->meshArena) cudaFree(C->meshArena);
     if (C->dMeshPtr) cudaFree(C->dMeshPtr);
     if (C->stream) cudaStreamDestroy(C->stream);
@@ -837,7 +909,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
         cudaStream_t st = cases[0]->stream;
         std::vector<double> stage;
         std::vector<btm::DevInst> hostInsts;
-        std::vector<int> blockIdx, gridIdx;
+        std::vector<int> blockIdx, gridIdx, mixIdx;
         std::vector<std::vector<double>> histBufs(n);
         std::vector<double *> histDev(n, nullptr);
         for (int i = 0; i < n; ++i) {
@@ -857,26 +929,49 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                 I.histCap = hists[i].residual_capacity;
             }
             ck(cudaMemsetAsync(I.barrier, 0, 512, st), "memset control");
-            if (J.C->nC <= block_max_cells()) blockIdx.push_back(i);
-            else gridIdx.push_back(i);
+            const bool mixed = J.C->settings.precision == BTM_PREC_MIXED;
+            if (mixed) {
+                if (J.C->nC > block_max_cells())
+                    throw BtmError(BTM_ERR_ARG, "mixed precision runs meshes of up to " +
+                                                    std::to_string(block_max_cells()) +
+                                                    " cells (one CTA per instance); use fp64 for larger meshes");
+                ensure_mixed(J.C, *J.S);
+                mixIdx.push_back(i);
+            } else if (J.C->nC <= block_max_cells()) {
+                blockIdx.push_back(i);
+            } else {
+                gridIdx.push_back(i);
+            }
         }
-        // one persistent launch for all block-mode instances
+        // one persistent launch per engine for all block-mode instances
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         ck(cudaEventCreate(&ev0), "event");
         ck(cudaEventCreate(&ev1), "event");
         btm::DevInst *dInsts = nullptr;
-        if (!blockIdx.empty()) {
+        const size_t nBlock = blockIdx.size() + mixIdx.size();
+        if (nBlock > 0) {
             std::vector<btm::DevInst> arr;
             for (int i : blockIdx) arr.push_back(jobs[i].S->inst);
+            for (int i : mixIdx) arr.push_back(jobs[i].S->inst);
             ck(cudaMalloc((void **)&dInsts, sizeof(btm::DevInst) * arr.size()), "cudaMalloc(insts)");
             ck(cudaMemcpyAsync(dInsts, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
-            int maxCells = 0;
-            for (int i : blockIdx) maxCells = std::max(maxCells, jobs[i].C->nC);
             ck(cudaEventRecord(ev0, st), "event");
-            int e = btm::engine_launch_block(dInsts, (int)arr.size(), block_threads_for(maxCells), st);
-            if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
+            if (!blockIdx.empty()) {
+                int maxCells = 0;
+                for (int i : blockIdx) maxCells = std::max(maxCells, jobs[i].C->nC);
+                int e = btm::engine_launch_block(dInsts, (int)blockIdx.size(), block_threads_for(maxCells), st);
+                if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
+            }
+            if (!mixIdx.empty()) {
+                int maxCells = 0;
+                for (int i : mixIdx) maxCells = std::max(maxCells, jobs[i].C->nC);
+                int e = btm::mixed_launch_block(dInsts + blockIdx.size(), (int)mixIdx.size(),
+                                                block_threads_for(maxCells), st);
+                if (e) throw BtmError(BTM_ERR_CUDA, std::string("mixed launch: ") + cudaGetErrorString((cudaError_t)e));
+            }
+        } else {
+            ck(cudaEventRecord(ev0, st), "event");
         }
-        if (blockIdx.empty()) ck(cudaEventRecord(ev0, st), "event");
         std::vector<btm::DevInst *> gridPtrs;
         for (int i : gridIdx) {
             btm::DevInst *dI = nullptr;
@@ -895,19 +990,26 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
         if (dInsts) cudaFree(dInsts);
         for (auto *p : gridPtrs) cudaFree(p);
         if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, std::string("solve: ") + cudaGetErrorString(se));
+        // per-instance device timestamps: [8] start, [9] end of each solve
+        std::vector<std::array<uint64_t, 10>> times(n);
+        uint64_t t0 = 0;
+        for (int i = 0; i < n; ++i) {
+            ck(cudaMemcpy(times[i].data(), jobs[i].S->inst.outTime, sizeof(uint64_t) * 10, cudaMemcpyDeviceToHost),
+               "status");
+            if (times[i][8] && (!t0 || times[i][8] < t0)) t0 = times[i][8];
+        }
         for (int i = 0; i < n; ++i) {
             Job &J = jobs[i];
             const btm::DevInst &I = J.S->inst;
             int32_t outv[8];
-            int64_t innerv = 0;
+            int64_t innerv[5] = {0, 0, 0, 0, 0};
             int32_t errv = 0;
             double lastv[6];
             ck(cudaMemcpy(outv, I.out, sizeof outv, cudaMemcpyDeviceToHost), "status");
-            ck(cudaMemcpy(&innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost), "status");
+            ck(cudaMemcpy(innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost), "status");
             ck(cudaMemcpy(lastv, I.outLast, sizeof lastv, cudaMemcpyDeviceToHost), "status");
             ck(cudaMemcpy(&errv, I.err, sizeof errv, cudaMemcpyDeviceToHost), "status");
-            uint64_t tns[8];
-            ck(cudaMemcpy(tns, I.outTime, sizeof tns, cudaMemcpyDeviceToHost), "status");
+            const uint64_t *tns = times[i].data();
             if (hists) {
                 btm_history &h = hists[i];
                 h.status = outv[0];
@@ -915,9 +1017,13 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                 h.diverged = outv[2];
                 h.final_iter = outv[3];
                 h.iterations_run = outv[4];
-                h.inner_iterations = innerv;
+                h.inner_iterations = innerv[0];
+                for (int q = 0; q < 4; ++q) h.inner_split[q] = innerv[q + 1];
+                h.polish_start = outv[7];
                 for (int q = 0; q < 6; ++q) h.last_residual[q] = lastv[q];
                 for (int q = 0; q < 8; ++q) h.phase_ms[q] = 1e-6 * (double)tns[q];
+                h.solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
+                h.finish_ms = (t0 && tns[9] > t0) ? 1e-6 * (double)(tns[9] - t0) : 0.0;
                 if (histDev[i]) {
                     int rows = std::min(h.residual_capacity, outv[4]);
                     ck(cudaMemcpy(h.residuals, histDev[i], sizeof(double) * 6 * rows, cudaMemcpyDeviceToHost), "hist");

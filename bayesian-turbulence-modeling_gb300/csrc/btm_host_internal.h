@@ -16,7 +16,9 @@
 struct Slab {
     void *dptr = nullptr;
     size_t bytes = 0;
-    btm::DevInst inst{};   // host copy with device pointers
+    void *dptr32 = nullptr;   // FP32 bulk of the mixed-precision engine (allocated on first use)
+    size_t bytes32 = 0;
+    btm::DevInst inst{};      // host copy with device pointers
 };
 
 struct btm_case {

@@ -1,0 +1,1378 @@
+// btm_mixed.cu - the mixed-precision SIMPLE / SST k-omega engine (sm_103a).
+//
+// The outer iteration is the reference's (incompressible/src/SIMPLESolver.cpp:
+// 731-1036, the same phase order as btm_engine.cu), restated in correction
+// form so that the bulk of the arithmetic runs in FP32 while the fixed point
+// remains that of the FP64 discrete equations:
+//   * the flow state U, p, k, omega and its boundary values stay FP64;
+//   * every equation is assembled in FP32 (coefficients, sources, closure
+//     fields, gradients); its defect r = b - A x is then evaluated in FP64
+//     against the FP64 state, and the FP32 Krylov / AMG solvers compute the
+//     correction A_relaxed dx = r that is added to the FP64 state.  Because
+//     b - A_relaxed x_old = b - A x_old exactly (the under-relaxation terms
+//     cancel), the defect is the reference's "initial residual" and the
+//     correction is the reference's relaxed update;
+//   * the continuity defect (face mass fluxes and their cell sums) is FP64,
+//     and the FP32 pressure-correction solve is refined against it in FP64;
+//   * Green-Gauss gradients use the difference form
+//     sum_f (phi_f - phi_P) S_f / V with phi_N - phi_P taken in FP64 (equal to
+//     sum_f phi_f S_f / V for closed cells), so FP32 rounding never meets the
+//     cancellation of sum_f phi_f S_f;
+//   * every correction system is solved with its right-hand side scaled to
+//     unit norm, so the FP32 breakdown guards and ranges stay meaningful as
+//     the defects shrink;
+//   * the cross-warp part of every Krylov dot product is accumulated in FP64.
+// A converged solve satisfies the FP64 discrete equations built from
+// FP32-rounded coefficients (relative perturbations of order 1e-7).
+#include "btm_common.h"
+#include "btm_team.cuh"
+#include "btm_bc.cuh"
+#include "btm_phases64.cuh"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace btm {
+
+// ---------------------------------------------------------------------------
+// SST point functions in FP32 (core/src/SSTModel.cpp:9-96)
+// ---------------------------------------------------------------------------
+struct CoefF {
+    float sk1, sw1, b1, al1, sk2, sw2, b2, al2, bstar, a1;
+    int variant;
+};
+__device__ __forceinline__ CoefF load_coef_f(const DevInst &I) {
+    CoefF c;
+    c.sk1 = (float)I.coeff[0]; c.sw1 = (float)I.coeff[1]; c.b1 = (float)I.coeff[2]; c.al1 = (float)I.coeff[3];
+    c.sk2 = (float)I.coeff[4]; c.sw2 = (float)I.coeff[5]; c.b2 = (float)I.coeff[6]; c.al2 = (float)I.coeff[7];
+    c.bstar = (float)I.coeff[8]; c.a1 = (float)I.coeff[9];
+    c.variant = I.variant;
+    return c;
+}
+__device__ __forceinline__ float blendf(float p1, float p2, float F1) { return F1 * p1 + (1.0f - F1) * p2; }
+
+__device__ __forceinline__ float sstf_F1(const CoefF &c, float k, float omega, float y, float nu, float CDpos) {
+    float kp = smaxf(k, 0.0f);
+    float sqrtK = sqrtf(kp);
+    float omSafe = smaxf(omega, 1e-20f);
+    float ySafe = smaxf(y, 1e-20f);
+    float y2s = ySafe * ySafe;
+    float term1 = sqrtK / (c.bstar * omSafe * ySafe);
+    float term2 = 500.0f * nu / (y2s * omSafe);
+    float term3 = 4.0f * c.sw2 * kp / (smaxf(CDpos, 1e-20f) * y2s);
+    float arg1 = sminf(smaxf(term1, term2), term3);
+    float a2 = arg1 * arg1;
+    return tanhf(a2 * a2);
+}
+__device__ __forceinline__ float sstf_F2(const CoefF &c, float k, float omega, float y, float nu) {
+    float sqrtK = sqrtf(smaxf(k, 0.0f));
+    float omSafe = smaxf(omega, 1e-20f);
+    float ySafe = smaxf(y, 1e-20f);
+    float term1 = 2.0f * sqrtK / (c.bstar * omSafe * ySafe);
+    float term2 = 500.0f * nu / (ySafe * ySafe * omSafe);
+    float arg2 = smaxf(term1, term2);
+    return tanhf(arg2 * arg2);
+}
+__device__ __forceinline__ float sstf_nut(const CoefF &c, float k, float omega, float S, float F2) {
+    float kSafe = smaxf(k, 0.0f);
+    if (c.variant == 1) return kSafe / smaxf(omega, 1e-20f);
+    float denom = smaxf(smaxf(c.a1 * omega, S * F2), 1e-20f);
+    return c.a1 * kSafe / denom;
+}
+__device__ __forceinline__ float sstf_Pk(const CoefF &c, float nuT, float S, float k, float omega) {
+    return sminf(nuT * S * S, 10.0f * c.bstar * smaxf(k, 0.0f) * smaxf(omega, 1e-20f));
+}
+__device__ __forceinline__ float sstf_Pw(const CoefF &c, float nuT, float S, float k, float omega) {
+    float lim = 10.0f * c.bstar * smaxf(k, 0.0f) * smaxf(omega, 1e-20f) / smaxf(nuT, 1e-30f);
+    return sminf(S * S, lim);
+}
+
+// ---------------------------------------------------------------------------
+// Green-Gauss gradients in difference form (core/include/Field.hpp:122-152):
+// g = (1/V) [sum_internal (phi_f - phi_P) S_f + sum_boundary (phi_b - phi_P) S_b]
+// with phi_f - phi_P = (1 - w)(phi_N - phi_P) seen from the owner and
+// w (phi_O - phi_P) seen from the neighbour.  V is the value type of the field
+// (double for the FP64 state, float for the pressure correction).
+// ---------------------------------------------------------------------------
+template <class T, int NF, class V>
+__device__ __forceinline__ void ggd_cell(const DevMesh &M, int c, const V *const *phi, const V *const *phib,
+                                         float *gx, float *gy, float *gz) {
+    const DevGeom32 &G = M.g32;
+    V pc[NF];
+    float ax[NF], ay[NF], az[NF];
+#pragma unroll
+    for (int q = 0; q < NF; ++q) { ax[q] = 0.0f; ay[q] = 0.0f; az[q] = 0.0f; pc[q] = LD(phi[q] + c); }
+    const int e0 = M.cfOff[c], e1 = M.cfOff[c + 1];
+    for (int e = e0; e < e1; ++e) {
+        const int f = M.cfFace[e];
+        const int oth = M.cfOther[e];
+        const float nx = G.nx[f], ny = G.ny[f], nz = G.nz[f];
+        float fac;
+        int other;
+        if (oth >= 0) { fac = (1.0f - G.w[f]) * G.area[f]; other = oth; }
+        else { fac = -G.w[f] * G.area[f]; other = -(oth + 1); }
+#pragma unroll
+        for (int q = 0; q < NF; ++q) {
+            const float d = (float)(LD(phi[q] + other) - pc[q]) * fac;
+            ax[q] = fmaf(d, nx, ax[q]);
+            ay[q] = fmaf(d, ny, ay[q]);
+            az[q] = fmaf(d, nz, az[q]);
+        }
+    }
+    for (int e = M.cbOff[c]; e < M.cbOff[c + 1]; ++e) {
+        const int b = M.cbFace[e];
+        const float fac = G.barea[b], nx = G.bnx[b], ny = G.bny[b], nz = G.bnz[b];
+#pragma unroll
+        for (int q = 0; q < NF; ++q) {
+            const float d = (float)(LD(phib[q] + b) - pc[q]) * fac;
+            ax[q] = fmaf(d, nx, ax[q]);
+            ay[q] = fmaf(d, ny, ay[q]);
+            az[q] = fmaf(d, nz, az[q]);
+        }
+    }
+    const float rv = G.rvol[c];
+#pragma unroll
+    for (int q = 0; q < NF; ++q) { gx[q] = ax[q] * rv; gy[q] = ay[q] * rv; gz[q] = az[q] * rv; }
+}
+
+// velocity gradients into f.g: which = bit mask of components (7 all, 3 x and y)
+template <class T>
+__device__ __noinline__ void mx_velgrad(T &tm, const DevMesh &M, DevInst &I, int which) {
+    DevWork32 &F = I.f;
+    const double *U[3] = {I.ux, I.uy, I.uz};
+    const double *UB[3] = {I.ubx, I.uby, I.ubz};
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        if (which == 7) {
+            float gx[3], gy[3], gz[3];
+            ggd_cell<T, 3, double>(M, c, U, UB, gx, gy, gz);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) { F.g[3 * i][c] = gx[i]; F.g[3 * i + 1][c] = gy[i]; F.g[3 * i + 2][c] = gz[i]; }
+        } else if (which == 3) {
+            float gx[2], gy[2], gz[2];
+            ggd_cell<T, 2, double>(M, c, U, UB, gx, gy, gz);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) { F.g[3 * i][c] = gx[i]; F.g[3 * i + 1][c] = gy[i]; F.g[3 * i + 2][c] = gz[i]; }
+        } else {
+            for (int i = 0; i < 3; ++i) {
+                if (!(which & (1 << i))) continue;
+                const double *P[1] = {U[i]};
+                const double *PB[1] = {UB[i]};
+                float gx[1], gy[1], gz[1];
+                ggd_cell<T, 1, double>(M, c, P, PB, gx, gy, gz);
+                F.g[3 * i][c] = gx[0]; F.g[3 * i + 1][c] = gy[0]; F.g[3 * i + 2][c] = gz[0];
+            }
+        }
+    }
+}
+
+template <class T>
+__device__ __noinline__ void mx_pgrad(T &tm, const DevMesh &M, DevInst &I) {
+    DevWork32 &F = I.f;
+    const double *P[1] = {I.p};
+    const double *PB[1] = {I.pb};
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        float gx[1], gy[1], gz[1];
+        ggd_cell<T, 1, double>(M, c, P, PB, gx, gy, gz);
+        F.gp[0][c] = gx[0]; F.gp[1][c] = gy[0]; F.gp[2][c] = gz[0];
+    }
+}
+
+// SSTModel::computeFields + |S| + start-up floor (SIMPLESolver.cpp:736-768) in FP32
+template <class T>
+__device__ __noinline__ void mx_sst(T &tm, const DevMesh &M, DevInst &I, float nutMin) {
+    const CoefF cf = load_coef_f(I);
+    const float nu = (float)I.nu;
+    DevWork32 &F = I.f;
+    const double *P[2] = {I.k, I.om};
+    const double *PB[2] = {I.kb, I.omb};
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        float S11 = F.g[0][c], S22 = F.g[4][c], S33 = F.g[8][c];
+        float S12 = 0.5f * (F.g[1][c] + F.g[3][c]);
+        float S13 = 0.5f * (F.g[2][c] + F.g[6][c]);
+        float S23 = 0.5f * (F.g[5][c] + F.g[7][c]);
+        float Sc = sqrtf(2.0f * (S11 * S11 + S22 * S22 + S33 * S33 + 2.0f * (S12 * S12 + S13 * S13 + S23 * S23)));
+        float gx[2], gy[2], gz[2];
+        ggd_cell<T, 2, double>(M, c, P, PB, gx, gy, gz);
+        float kc = smaxf((float)LD(I.k + c), 0.0f);
+        float wc = smaxf((float)LD(I.om + c), 1e-20f);
+        float y = smaxf(M.g32.wd[c], 1e-20f);
+        float CDkw = 2.0f * cf.sw2 / wc * (gx[0] * gx[1] + gy[0] * gy[1] + gz[0] * gz[1]);
+        float F1 = (cf.variant == 2) ? 1.0f : sstf_F1(cf, kc, wc, y, nu, smaxf(CDkw, 1e-20f));
+        float F2 = sstf_F2(cf, kc, wc, y, nu);
+        float nuT = sstf_nut(cf, kc, wc, Sc, F2);
+        F.smag[c] = Sc;
+        F.cdkw[c] = CDkw;
+        F.f1[c] = F1;
+        F.f2[c] = F2;
+        F.pk[c] = sstf_Pk(cf, nuT, Sc, kc, wc);
+        F.nut[c] = (nutMin < 0.0f) ? nuT : smaxf(nuT, nutMin);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// assembly in FP32, defects in FP64 (SIMPLESolver.cpp:56-203, 322-450, 483-669)
+// ---------------------------------------------------------------------------
+// FP64 face mass flux (U_f . n) A from the FP64 state (interpolation weights,
+// normals and areas in FP64); the z term is skipped when U_z is identically 0
+template <class T>
+__device__ __forceinline__ double mflux64(const DevMesh &M, const DevInst &I, int f, int o, int n, bool z) {
+    const double w = M.w[f], wn = 1.0 - w;
+    double m = (LD(I.ux + o) * w + LD(I.ux + n) * wn) * M.nx[f];
+    m = fma(LD(I.uy + o) * w + LD(I.uy + n) * wn, M.ny[f], m);
+    if (z) m = fma(LD(I.uz + o) * w + LD(I.uz + n) * wn, M.nz[f], m);
+    return m * M.area[f];
+}
+template <class T>
+__device__ __forceinline__ double bflux64(const DevMesh &M, const DevInst &I, int b, bool z) {
+    double m = LD(I.ubx + b) * M.bnx[b];
+    m = fma(LD(I.uby + b), M.bny[b], m);
+    if (z) m = fma(LD(I.ubz + b), M.bnz[b], m);
+    return m * M.barea[b];
+}
+
+// Convection-diffusion face pass shared by momentum and k / omega: FP64 mass
+// flux into f.mflux (when `flux`), FP32 diffusion coefficient into f.dcoef and
+// the upwind LDU coefficients (signs from the FP64 flux).  sigma-blending by
+// the face F1 when `sg1 >= 0` (k / omega), plain nu + nu_t otherwise.
+template <class T>
+__device__ __forceinline__ void cd_face(const DevMesh &M, DevInst &I, int f, float nu, float sg1, float sg2,
+                                        bool flux, bool z, float &w, float &wn, int &o, int &n) {
+    const DevGeom32 &G = M.g32;
+    DevWork32 &F = I.f;
+    o = M.own[f];
+    n = M.nbr[f];
+    w = G.w[f];
+    wn = 1.0f - w;
+    const float nuo = F.nut[o], nun = F.nut[n];
+    float Df;
+    if (sg1 >= 0.0f) {
+        const float sg = blendf(sg1, sg2, w * F.f1[o] + wn * F.f1[n]);
+        Df = (w * (nu + sg * nuo) + wn * (nu + sg * nun)) * G.area[f] * G.rdelta[f];
+    } else {
+        Df = (w * (nu + nuo) + wn * (nu + nun)) * G.area[f] * G.rdelta[f];
+    }
+    double m;
+    if (flux) {
+        m = mflux64<T>(M, I, f, o, n, z);
+        F.mflux[f] = m;
+    } else {
+        m = LD(F.mflux + f);
+    }
+    const float m32 = (float)m;
+    F.dcoef[f] = Df;
+    F.upper[f] = -(Df + smaxf(-m32, 0.0f));
+    F.lower[f] = -(Df + smaxf(m32, 0.0f));
+}
+
+// momentum face pass (component `comp`): convection-diffusion coefficients
+// and the transpose-stress face flux
+template <class T>
+__device__ __noinline__ void mx_mom_faces(T &tm, const DevMesh &M, DevInst &I, int comp) {
+    const DevGeom32 &G = M.g32;
+    DevWork32 &F = I.f;
+    const float nu = (float)I.nu;
+    const bool z = I.solveZ != 0;
+    const float *gc0 = F.g[comp], *gc1 = F.g[3 + comp], *gc2 = F.g[6 + comp];
+    for (int f = tm.rank(); f < M.nIF; f += tm.size()) {
+        float w, wn;
+        int o, n;
+        cd_face<T>(M, I, f, nu, -1.0f, 0.0f, true, z, w, wn, o, n);
+        const float cfac = w * F.nut[o] + wn * F.nut[n];
+        const float gx = gc0[o] * w + gc0[n] * wn, gy = gc1[o] * w + gc1[n] * wn, gz = gc2[o] * w + gc2[n] * wn;
+        F.tflux[f] = cfac * (gx * G.nx[f] + gy * G.ny[f] + gz * G.nz[f]) * G.area[f];
+    }
+}
+
+// Convective-diffusive defect of one cell in conservative flux form,
+//   sum_f [ D_f (phi_P - phi_N) + mdot_f,out * phi_upwind ],
+// FP64 differences and FP64 mass fluxes, so the large convective terms cancel
+// exactly as in the reference instead of through FP32-rounded coefficients.
+// Also accumulates the FP32 diagonal (sum of the row's face coefficients).
+template <class T>
+__device__ __forceinline__ double cd_cell_flux(const DevMesh &M, const DevInst &I, int c, const double *phi,
+                                               double phiP, float &diag) {
+    const DevWork32 &F = I.f;
+    double r = 0.0;
+    for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
+        const int f = M.cfFace[e], oth = M.cfOther[e];
+        int other;
+        double mo;
+        if (oth >= 0) {
+            diag -= F.lower[f];
+            other = oth;
+            mo = LD(F.mflux + f);
+        } else {
+            diag -= F.upper[f];
+            other = -(oth + 1);
+            mo = -LD(F.mflux + f);
+        }
+        const double phiN = LD(phi + other);
+        r = fma((double)F.dcoef[f], phiP - phiN, r);
+        r = fma(mo, mo >= 0.0 ? phiP : phiN, r);
+    }
+    return r;
+}
+
+// momentum cell pass: FP32 relaxed diagonal; FP64 defect of the unrelaxed
+// equation, b - A u, into f.src.  Returns this thread's share of |defect|^2.
+template <class T>
+__device__ __noinline__ double mx_mom_cells(T &tm, const DevMesh &M, DevInst &I, int comp) {
+    const DevGeom32 &G = M.g32;
+    DevWork32 &F = I.f;
+    const float nu = (float)I.nu;
+    const float alphaU = (float)I.S.alphaU;
+    const float fb = (float)I.S.bodyForce[comp];
+    const double *Uc = comp == 0 ? I.ux : (comp == 1 ? I.uy : I.uz);
+    const double *Ubc = comp == 0 ? I.ubx : (comp == 1 ? I.uby : I.ubz);
+    const float *gp = F.gp[comp];
+    const float *gc0 = F.g[comp], *gc1 = F.g[3 + comp], *gc2 = F.g[6 + comp];
+    const bool wallFn = I.S.useWallFn != 0;
+    const bool z = I.solveZ != 0;
+    double rr = 0.0;
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        const double uP = LD(Uc + c);
+        float diag = 0.0f, ts = 0.0f;
+        double flux = cd_cell_flux<T>(M, I, c, Uc, uP, diag);
+        for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
+            const int f = M.cfFace[e];
+            ts += M.cfOther[e] >= 0 ? F.tflux[f] : -F.tflux[f];
+        }
+        const float nutc = F.nut[c];
+        for (int e = M.cbOff[c]; e < M.cbOff[c + 1]; ++e) {
+            const int b = M.cbFace[e];
+            const float nuEff = (M.bwall[b] && !wallFn) ? nu : nu + nutc;
+            const float Db = nuEff * G.barea[b] * G.brdelta[b];
+            const double ub = LD(Ubc + b);
+            const double mb = bflux64<T>(M, I, b, z);
+            diag += (mb >= 0.0) ? (float)mb + Db : Db;
+            flux = fma((double)Db, uP - ub, flux);
+            flux = fma(mb, mb >= 0.0 ? uP : ub, flux);
+        }
+        const float gcx = gc0[c], gcy = gc1[c], gcz = gc2[c];
+        for (int e = M.cbpOff[c]; e < M.cbpOff[c + 1]; ++e) {
+            const int b = M.cbpFace[e];
+            const float cfac = M.bwall[b] ? 0.0f : nutc;
+            ts += cfac * (gcx * G.bnx[b] + gcy * G.bny[b] + gcz * G.bnz[b]) * G.barea[b];
+        }
+        const float vol = G.vol[c];
+        float src = ts - gp[c] * vol;
+        if (fb != 0.0f) src = fmaf(fb, vol, src);
+        const double rc = (double)src - flux;
+        rr = fma(rc, rc, rr);
+        F.src[c] = (float)rc;
+        const float dr = diag / alphaU;
+        F.diag[c] = dr;
+        if (comp == 0) F.aPx[c] = dr;
+    }
+    return rr;
+}
+
+// pressure-correction face pass: FP32 Laplacian coefficient, FP64 mass flux
+// with the (FP32) Rhie-Chow dissipation
+template <class T>
+__device__ __noinline__ void mx_p_faces(T &tm, const DevMesh &M, DevInst &I) {
+    const DevGeom32 &G = M.g32;
+    DevWork32 &F = I.f;
+    const bool rc = M.rhieChow != 0;
+    const bool z = I.solveZ != 0;
+    for (int f = tm.rank(); f < M.nIF; f += tm.size()) {
+        const int o = M.own[f], n = M.nbr[f];
+        const float Sf = G.area[f], w = G.w[f], wn = 1.0f - w;
+        const float aPo = F.aPx[o], aPn = F.aPx[n];
+        const float dP_o = (fabsf(aPo) > 1e-30f) ? G.vol[o] / aPo : 0.0f;
+        const float dP_n = (fabsf(aPn) > 1e-30f) ? G.vol[n] / aPn : 0.0f;
+        const float dP_f = w * dP_o + wn * dP_n;
+        const float coeff = dP_f * Sf * G.rdelta[f];
+        F.upper[f] = -coeff;
+        F.lower[f] = -coeff;
+        double mf = mflux64<T>(M, I, f, o, n, z);
+        if (rc) {
+            const float gbx = F.gp[0][o] * w + F.gp[0][n] * wn;
+            const float gby = F.gp[1][o] * w + F.gp[1][n] * wn;
+            const float gbz = F.gp[2][o] * w + F.gp[2][n] * wn;
+            const float dp = (float)(LD(I.p + n) - LD(I.p + o));
+            const float d = -dP_f * Sf * (dp * G.rdelta[f] - (gbx * G.ex[f] + gby * G.ey[f] + gbz * G.ez[f]));
+            mf += (double)d;
+        }
+        F.mflux[f] = mf;
+    }
+}
+
+// pressure-correction cell pass: FP64 continuity defect (the right-hand side)
+template <class T>
+__device__ __noinline__ double mx_p_cells(T &tm, const DevMesh &M, DevInst &I) {
+    const DevGeom32 &G = M.g32;
+    DevWork32 &F = I.f;
+    const bool z = I.solveZ != 0;
+    double rr = 0.0;
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        float diag = 0.0f;
+        double src = 0.0;
+        for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
+            const int f = M.cfFace[e];
+            diag -= F.upper[f];
+            if (M.cfOther[e] >= 0) src -= LD(F.mflux + f);
+            else src += LD(F.mflux + f);
+        }
+        const float aPc = F.aPx[c];
+        for (int e = M.cbpOff[c]; e < M.cbpOff[c + 1]; ++e) {
+            const int b = M.cbpFace[e];
+            src -= bflux64<T>(M, I, b, z);
+            if (M.bout[b]) {
+                const float dP_o = (fabsf(aPc) > 1e-30f) ? G.vol[c] / aPc : 0.0f;
+                diag += dP_o * G.barea[b] * G.brdelta[b];
+            }
+        }
+        if (!M.hasOutlet && c == 0) diag += fabsf(diag) > 1e-30f ? diag : 1.0f;
+        F.diag[c] = diag;
+        F.src64[c] = src;
+        F.src[c] = (float)src;
+        F.pp[c] = 0.0f;
+        rr = fma(src, src, rr);
+    }
+    return rr;
+}
+
+// k (which = 0) or omega (which = 1) face pass; omega reuses the mass flux of
+// the k pass (U does not change between the two)
+template <class T>
+__device__ __noinline__ void mx_turb_faces(T &tm, const DevMesh &M, DevInst &I, int which) {
+    const CoefF cf = load_coef_f(I);
+    const float nu = (float)I.nu;
+    const float s1 = which == 0 ? cf.sk1 : cf.sw1, s2 = which == 0 ? cf.sk2 : cf.sw2;
+    const bool z = I.solveZ != 0;
+    for (int f = tm.rank(); f < M.nIF; f += tm.size()) {
+        float w, wn;
+        int o, n;
+        cd_face<T>(M, I, f, nu, s1, s2, which == 0, z, w, wn, o, n);
+    }
+}
+
+template <class T>
+__device__ __noinline__ double mx_turb_cells(T &tm, const DevMesh &M, DevInst &I, int which) {
+    const CoefF cf = load_coef_f(I);
+    const DevGeom32 &G = M.g32;
+    DevWork32 &F = I.f;
+    const float nu = (float)I.nu;
+    const float s1 = which == 0 ? cf.sk1 : cf.sw1, s2 = which == 0 ? cf.sk2 : cf.sw2;
+    const double *phib = which == 0 ? I.kb : I.omb;
+    const double *phi = which == 0 ? I.k : I.om;
+    const float alpha = (float)(which == 0 ? I.S.alphaK : I.S.alphaW);
+    const bool z = I.solveZ != 0;
+    double rr = 0.0;
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        const double phiP = LD(phi + c);
+        float diag = 0.0f;
+        double flux = cd_cell_flux<T>(M, I, c, phi, phiP, diag);
+        const float F1c = F.f1[c], nutc = F.nut[c];
+        const float sg = blendf(s1, s2, F1c);
+        for (int e = M.cbOff[c]; e < M.cbOff[c + 1]; ++e) {
+            const int b = M.cbFace[e];
+            const float Db = (nu + sg * nutc) * G.barea[b] * G.brdelta[b];
+            const double vb = LD(phib + b);
+            const double mb = bflux64<T>(M, I, b, z);
+            diag += (mb >= 0.0) ? (float)mb + Db : Db;
+            flux = fma((double)Db, phiP - vb, flux);
+            flux = fma(mb, mb >= 0.0 ? phiP : vb, flux);
+        }
+        const float vol = G.vol[c];
+        const float omc = (float)LD(I.om + c);
+        float src, sink;
+        if (which == 0) {
+            src = F.pk[c] * vol;
+            sink = cf.bstar * smaxf(omc, 1e-20f) * vol;
+        } else {
+            const float alphaB = blendf(cf.al1, cf.al2, F1c);
+            src = alphaB * sstf_Pw(cf, nutc, F.smag[c], (float)LD(I.k + c), omc) * vol;
+            src += (1.0f - F1c) * F.cdkw[c] * vol;
+            sink = blendf(cf.b1, cf.b2, F1c) * smaxf(omc, 1e-20f) * vol;
+        }
+        diag += sink;
+        const double rc = (double)src - fma((double)sink, phiP, flux);
+        rr = fma(rc, rc, rr);
+        F.src[c] = (float)rc;
+        F.diag[c] = diag / alpha;
+    }
+    return rr;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 linear algebra on the correction systems (core/include/LinearSolver.hpp)
+// The system is (f.diag, f.upper, f.lower) with right-hand side f.src * scale
+// and zero initial guess (a correction).  Breakdown guards are the
+// reference's absolute 1e-30, meaningful because the right-hand side is
+// scaled to unit norm.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ float ldu_rowf(const DevMesh &M, const DevWork32 &F, const float *x, int c) {
+    float y = LD(F.diag + c) * LD(x + c);
+    for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
+        const int f = M.cfFace[e], oth = M.cfOther[e];
+        if (oth >= 0) y = fmaf(LD(F.upper + f), LD(x + oth), y);
+        else y = fmaf(LD(F.lower + f), LD(x + (-(oth + 1))), y);
+    }
+    return y;
+}
+__device__ __forceinline__ float jac_rdf(float d) { return (fabsf(d) > 1e-30f) ? 1.0f / d : 1.0f; }
+__device__ __forceinline__ float gs_rdf(float d) { return (fabsf(d) > 1e-30f) ? 1.0f / d : 0.0f; }
+
+struct SolveResF {
+    int iterations;
+    float finalRes;
+    int converged;
+};
+
+// BiCGSTABSolver::solve (LinearSolver.hpp:191-247), right Jacobi preconditioned
+template <class T>
+__device__ __noinline__ SolveResF mx_bicgstab(T &tm, const DevMesh &M, DevWork32 &F, float *x, float scale,
+                                              int maxIter, float tol) {
+    SolveResF res = {0, 0.0f, 0};
+    const int nC = M.nC;
+    float a0[1] = {0.0f};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const float rc = LD(F.src + c) * scale;
+        F.r[c] = rc; F.rh[c] = rc; F.pv[c] = 0.0f; F.v[c] = 0.0f;
+        F.rd[c] = jac_rdf(LD(F.diag + c));
+        x[c] = 0.0f;
+        a0[0] = fmaf(rc, rc, a0[0]);
+    }
+    tm.template sumf<1>(a0);
+    const float r0 = sqrtf(a0[0]);
+    if (r0 < 1e-30f) { res.converged = 1; return res; }
+    float rhoN = a0[0];
+    float rho = 1.0f, alpha = 1.0f, omega = 1.0f;
+    for (int it = 0; it < maxIter; ++it) {
+        if (!tm.ok()) break;
+        if (fabsf(rhoN) < 1e-30f) break;
+        const float beta = (rhoN / (rho + 1e-30f)) * (alpha / (omega + 1e-30f));
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const float p = fmaf(beta, fmaf(-omega, LD(F.v + c), LD(F.pv + c)), LD(F.r + c));
+            F.pv[c] = p;
+            F.ph[c] = p * LD(F.rd + c);
+        }
+        tm.sync();
+        float a1[1] = {0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const float vc = ldu_rowf<T>(M, F, F.ph, c);
+            F.v[c] = vc;
+            a1[0] = fmaf(LD(F.rh + c), vc, a1[0]);
+        }
+        tm.template sumf<1>(a1);
+        const float rv = a1[0];
+        if (fabsf(rv) < 1e-30f) break;
+        alpha = rhoN / rv;
+        float a2[1] = {0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const float sc = fmaf(-alpha, LD(F.v + c), LD(F.r + c));
+            F.s[c] = sc;
+            F.sh[c] = sc * LD(F.rd + c);
+            a2[0] = fmaf(sc, sc, a2[0]);
+        }
+        tm.template sumf<1>(a2);
+        const float sn = sqrtf(a2[0]);
+        if (sn / r0 < tol) {
+            for (int c = tm.rank(); c < nC; c += tm.size()) x[c] = fmaf(alpha, LD(F.ph + c), x[c]);
+            res.iterations = it + 1; res.finalRes = sn / r0; res.converged = 1;
+            return res;
+        }
+        float a3[2] = {0.0f, 0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const float tc = ldu_rowf<T>(M, F, F.sh, c);
+            F.t[c] = tc;
+            a3[0] = fmaf(tc, tc, a3[0]);
+            a3[1] = fmaf(tc, LD(F.s + c), a3[1]);
+        }
+        tm.template sumf<2>(a3);
+        const float tt = a3[0];
+        omega = (tt > 1e-30f) ? a3[1] / tt : 0.0f;
+        float a4[2] = {0.0f, 0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            x[c] = x[c] + fmaf(alpha, LD(F.ph + c), omega * LD(F.sh + c));
+            const float rc = fmaf(-omega, LD(F.t + c), LD(F.s + c));
+            F.r[c] = rc;
+            a4[0] = fmaf(rc, rc, a4[0]);
+            a4[1] = fmaf(LD(F.rh + c), rc, a4[1]);
+        }
+        tm.template sumf<2>(a4);
+        const float rn = sqrtf(a4[0]);
+        res.iterations = it + 1;
+        res.finalRes = rn / r0;
+        if (res.finalRes < tol) { res.converged = 1; return res; }
+        if (fabsf(omega) < 1e-30f) break;
+        rho = rhoN;
+        rhoN = a4[1];
+    }
+    return res;
+}
+
+// ---- pressure AMG in FP32 (hierarchy structure shared with the FP64 engine) --
+__device__ __forceinline__ float *lev_valsf(DevWork32 &F, const DevMesh &M, int l) {
+    return l == 0 ? F.diag : F.amgVal + M.lev[l].valOff;
+}
+__device__ __forceinline__ float *lev_xf(DevWork32 &F, const DevMesh &M, int l) {
+    return l == 0 ? F.s : F.amgX + M.lev[l].vecOff;
+}
+__device__ __forceinline__ float *lev_bf(DevWork32 &F, const DevMesh &M, int l) {
+    return l == 0 ? F.r : F.amgB + M.lev[l].vecOff;
+}
+__device__ __forceinline__ float *lev_rf(DevWork32 &F, const DevMesh &M, int l) {
+    return l == 0 ? F.t : F.amgR + M.lev[l].vecOff;
+}
+__device__ __forceinline__ float *lev_rdf(DevWork32 &F, const DevMesh &M, int l) {
+    return l == 0 ? F.amgRd : F.amgRd + M.nC + M.lev[l].vecOff;
+}
+
+template <class T>
+__device__ void mx_amg_galerkin(T &tm, const DevMesh &M, DevWork32 &F, int l) {
+    const AmgLevelDev &L = M.lev[l];
+    const float *fine = lev_valsf(F, M, l - 1);
+    float *val = lev_valsf(F, M, l);
+    for (int k = tm.rank(); k < L.nnz; k += tm.size()) {
+        float s = 0.0f;
+        for (int q = L.gOff[k]; q < L.gOff[k + 1]; ++q) s += LD(fine + L.gIdx[q]);
+        val[k] = s;
+    }
+}
+
+template <class T>
+__device__ void mx_amg_level_rd(T &tm, const DevMesh &M, DevWork32 &F, int l) {
+    const AmgLevelDev &L = M.lev[l];
+    float *rd = lev_rdf(F, M, l);
+    const float *val = lev_valsf(F, M, l);
+    for (int i = tm.rank(); i < L.n; i += tm.size()) {
+        float d;
+        if (l == 0) d = LD(F.diag + i);
+        else d = L.diagPos[i] >= 0 ? LD(val + L.diagPos[i]) : 0.0f;
+        rd[i] = gs_rdf(d);
+    }
+}
+
+// dense inverse of the coarsest level (Gauss-Jordan, ping-pong buffers)
+template <class T>
+__device__ __noinline__ void mx_amg_coarse_inverse(T &tm, const DevMesh &M, DevWork32 &F) {
+    const int l = M.nLevels - 1;
+    const AmgLevelDev &L = M.lev[l];
+    const int n = L.n, w2 = 2 * n;
+    float *A = F.gj, *B = F.gj + (size_t)n * w2;
+    const float *val = lev_valsf(F, M, l);
+    for (int i = tm.rank(); i < n; i += tm.size()) {
+        float *row = A + (size_t)i * w2;
+        for (int j = 0; j < w2; ++j) row[j] = 0.0f;
+        if (l == 0) {
+            row[i] = LD(F.diag + i);
+            for (int e = M.cfOff[i]; e < M.cfOff[i + 1]; ++e) {
+                const int f = M.cfFace[e], oth = M.cfOther[e];
+                if (oth >= 0) row[oth] = LD(F.upper + f);
+                else row[-(oth + 1)] = LD(F.lower + f);
+            }
+        } else {
+            for (int q = L.rowPtr[i]; q < L.rowPtr[i + 1]; ++q) row[L.colIdx[q]] = LD(val + q);
+        }
+        row[n + i] = 1.0f;
+    }
+    tm.sync();
+    for (int k = 0; k < n; ++k) {
+        const float piv = LD(A + (size_t)k * w2 + k);
+        const bool skip = !(fabsf(piv) > 1e-37f);
+        const float rp = skip ? 0.0f : 1.0f / piv;
+        for (int idx = tm.rank(); idx < n * w2; idx += tm.size()) {
+            const int i = idx / w2, j = idx - i * w2;
+            const float akj = LD(A + (size_t)k * w2 + j) * rp;
+            float v = LD(A + idx);
+            if (!skip) {
+                if (i == k) v = akj;
+                else v = fmaf(-LD(A + (size_t)i * w2 + k), akj, v);
+            }
+            B[idx] = v;
+        }
+        tm.sync();
+        float *tmp = A; A = B; B = tmp;
+    }
+    for (int idx = tm.rank(); idx < n * n; idx += tm.size()) {
+        const int i = idx / n, j = idx - i * n;
+        F.ainv[idx] = LD(A + (size_t)i * w2 + n + j);
+    }
+    tm.sync();
+}
+
+template <class T>
+__device__ __noinline__ void mx_amg_gs_sweep(T &tm, const DevMesh &M, DevWork32 &F, int l, bool reverse) {
+    const AmgLevelDev &L = M.lev[l];
+    float *x = lev_xf(F, M, l);
+    const float *b = lev_bf(F, M, l);
+    const float *val = lev_valsf(F, M, l);
+    const float *rd = lev_rdf(F, M, l);
+    for (int cc = 0; cc < L.nColors; ++cc) {
+        const int col = reverse ? L.nColors - 1 - cc : cc;
+        for (int q = L.colorOff[col] + tm.rank(); q < L.colorOff[col + 1]; q += tm.size()) {
+            const int i = L.colorRows[q];
+            const float ri = LD(rd + i);
+            if (ri == 0.0f) continue;
+            float s = LD(b + i);
+            if (l == 0) {
+                for (int e = M.cfOff[i]; e < M.cfOff[i + 1]; ++e) {
+                    const int f = M.cfFace[e], oth = M.cfOther[e];
+                    if (oth >= 0) s = fmaf(-LD(F.upper + f), LD(x + oth), s);
+                    else s = fmaf(-LD(F.lower + f), LD(x + (-(oth + 1))), s);
+                }
+            } else {
+                for (int q2 = L.rowPtr[i]; q2 < L.rowPtr[i + 1]; ++q2) {
+                    const int j = L.colIdx[q2];
+                    if (j != i) s = fmaf(-LD(val + q2), LD(x + j), s);
+                }
+            }
+            x[i] = s * ri;
+        }
+        tm.sync();
+    }
+}
+
+template <class T>
+__device__ __noinline__ void mx_amg_restrict(T &tm, const DevMesh &M, DevWork32 &F, int l) {
+    const AmgLevelDev &L = M.lev[l];
+    const float *x = lev_xf(F, M, l), *b = lev_bf(F, M, l), *val = lev_valsf(F, M, l);
+    float *r = lev_rf(F, M, l);
+    for (int i = tm.rank(); i < L.n; i += tm.size()) {
+        float s;
+        if (l == 0) {
+            s = ldu_rowf<T>(M, F, x, i);
+        } else {
+            s = 0.0f;
+            for (int q = L.rowPtr[i]; q < L.rowPtr[i + 1]; ++q) s = fmaf(LD(val + q), LD(x + L.colIdx[q]), s);
+        }
+        r[i] = LD(b + i) - s;
+    }
+    tm.sync();
+    const AmgLevelDev &C = M.lev[l + 1];
+    float *bc = lev_bf(F, M, l + 1), *xc = lev_xf(F, M, l + 1);
+    for (int J = tm.rank(); J < C.n; J += tm.size()) {
+        float s = 0.0f;
+        for (int q = L.aggOff[J]; q < L.aggOff[J + 1]; ++q) s += LD(r + L.aggMem[q]);
+        bc[J] = s;
+        xc[J] = 0.0f;
+    }
+    tm.sync();
+}
+
+template <class T>
+__device__ void mx_amg_prolong(T &tm, const DevMesh &M, DevWork32 &F, int l) {
+    const AmgLevelDev &L = M.lev[l];
+    float *x = lev_xf(F, M, l);
+    const float *xc = lev_xf(F, M, l + 1);
+    for (int i = tm.rank(); i < L.n; i += tm.size()) x[i] = LD(x + i) + LD(xc + L.map[i]);
+    tm.sync();
+}
+
+template <class T>
+__device__ void mx_amg_coarse_solve(T &tm, const DevMesh &M, DevWork32 &F) {
+    const int l = M.nLevels - 1;
+    const int n = M.lev[l].n;
+    if (M.coarseDirect) {
+        const float *b = lev_bf(F, M, l);
+        float *x = lev_xf(F, M, l);
+        for (int i = tm.rank(); i < n; i += tm.size()) {
+            float s = 0.0f;
+            for (int j = 0; j < n; ++j) s = fmaf(LD(F.ainv + (size_t)i * n + j), LD(b + j), s);
+            x[i] = s;
+        }
+        tm.sync();
+    } else {
+        for (int s = 0; s < kCoarseSweeps; ++s) mx_amg_gs_sweep(tm, M, F, l, (s & 1) != 0);
+    }
+}
+
+template <class T>
+__device__ void mx_amg_setup(T &tm, const DevMesh &M, DevWork32 &F) {
+    mx_amg_level_rd(tm, M, F, 0);
+    for (int l = 1; l < M.nLevels; ++l) {
+        mx_amg_galerkin(tm, M, F, l);
+        tm.sync();
+        mx_amg_level_rd(tm, M, F, l);
+    }
+    tm.sync();
+    if (M.coarseDirect) mx_amg_coarse_inverse(tm, M, F);
+}
+
+// symmetric V-cycle: 2 pre-sweeps (colours ascending), 2 post (descending)
+template <class T>
+__device__ void mx_amg_vcycle(T &tm, const DevMesh &M, DevWork32 &F) {
+    const int nl = M.nLevels;
+    for (int l = 0; l < nl - 1; ++l) {
+        mx_amg_gs_sweep(tm, M, F, l, false);
+        mx_amg_gs_sweep(tm, M, F, l, false);
+        mx_amg_restrict(tm, M, F, l);
+    }
+    mx_amg_coarse_solve(tm, M, F);
+    for (int l = nl - 2; l >= 0; --l) {
+        mx_amg_prolong(tm, M, F, l);
+        mx_amg_gs_sweep(tm, M, F, l, true);
+        mx_amg_gs_sweep(tm, M, F, l, true);
+    }
+}
+
+// AMG-preconditioned CG (AMGSolver::solve, LinearSolver.hpp:602-653):
+// r = f.r, z = f.s (V-cycle level-0 x), p = f.pv, Ap = f.v, V-cycle scratch f.t
+template <class T>
+__device__ __noinline__ SolveResF mx_amg_pcg(T &tm, const DevMesh &M, DevWork32 &F, float *x, float scale,
+                                             int maxIter, float tol, bool setup) {
+    SolveResF res = {0, 0.0f, 0};
+    const int nC = M.nC;
+    if (setup) mx_amg_setup(tm, M, F);
+    float a0[1] = {0.0f};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const float rc = LD(F.src + c) * scale;
+        F.r[c] = rc;
+        F.s[c] = 0.0f;
+        x[c] = 0.0f;
+        a0[0] = fmaf(rc, rc, a0[0]);
+    }
+    tm.template sumf<1>(a0);
+    const float r0 = sqrtf(a0[0]);
+    if (r0 < 1e-30f) { res.converged = 1; return res; }
+    mx_amg_vcycle(tm, M, F);
+    float a1[1] = {0.0f};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const float z = LD(F.s + c);
+        F.pv[c] = z;
+        a1[0] = fmaf(LD(F.r + c), z, a1[0]);
+    }
+    tm.template sumf<1>(a1);
+    float rz = a1[0];
+    for (int it = 0; it < maxIter; ++it) {
+        if (!tm.ok()) break;
+        float a2[1] = {0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const float ap = ldu_rowf<T>(M, F, F.pv, c);
+            F.v[c] = ap;
+            a2[0] = fmaf(LD(F.pv + c), ap, a2[0]);
+        }
+        tm.template sumf<1>(a2);
+        const float pAp = a2[0];
+        if (fabsf(pAp) < 1e-30f) break;
+        const float alpha = rz / pAp;
+        float a3[1] = {0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            x[c] = fmaf(alpha, LD(F.pv + c), x[c]);
+            const float rc = fmaf(-alpha, LD(F.v + c), LD(F.r + c));
+            F.r[c] = rc;
+            F.s[c] = 0.0f;
+            a3[0] = fmaf(rc, rc, a3[0]);
+        }
+        tm.template sumf<1>(a3);
+        const float rn = sqrtf(a3[0]);
+        res.iterations = it + 1;
+        res.finalRes = rn / r0;
+        if (res.finalRes < tol) { res.converged = 1; return res; }
+        mx_amg_vcycle(tm, M, F);
+        float a4[1] = {0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) a4[0] = fmaf(LD(F.r + c), LD(F.s + c), a4[0]);
+        tm.template sumf<1>(a4);
+        const float rzNew = a4[0];
+        const float beta = rzNew / (rz + 1e-30f);
+        for (int c = tm.rank(); c < nC; c += tm.size()) F.pv[c] = fmaf(beta, LD(F.pv + c), LD(F.s + c));
+        tm.sync();
+        rz = rzNew;
+    }
+    return res;
+}
+
+// Jacobi-preconditioned CG (PCGSolver::solve, LinearSolver.hpp:147-186)
+template <class T>
+__device__ __noinline__ SolveResF mx_pcg(T &tm, const DevMesh &M, DevWork32 &F, float *x, float scale, int maxIter,
+                                         float tol) {
+    SolveResF res = {0, 0.0f, 0};
+    const int nC = M.nC;
+    float a0[2] = {0.0f, 0.0f};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const float rc = LD(F.src + c) * scale;
+        const float rdc = jac_rdf(LD(F.diag + c));
+        const float z = rc * rdc;
+        F.rd[c] = rdc;
+        F.r[c] = rc; F.s[c] = z; F.pv[c] = z;
+        x[c] = 0.0f;
+        a0[0] = fmaf(rc, rc, a0[0]);
+        a0[1] = fmaf(rc, z, a0[1]);
+    }
+    tm.template sumf<2>(a0);
+    const float r0 = sqrtf(a0[0]);
+    if (r0 < 1e-30f) { res.converged = 1; return res; }
+    float rz = a0[1];
+    for (int it = 0; it < maxIter; ++it) {
+        if (!tm.ok()) break;
+        float a2[1] = {0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const float ap = ldu_rowf<T>(M, F, F.pv, c);
+            F.v[c] = ap;
+            a2[0] = fmaf(LD(F.pv + c), ap, a2[0]);
+        }
+        tm.template sumf<1>(a2);
+        const float pAp = a2[0];
+        if (fabsf(pAp) < 1e-30f) break;
+        const float alpha = rz / pAp;
+        float a3[2] = {0.0f, 0.0f};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            x[c] = fmaf(alpha, LD(F.pv + c), x[c]);
+            const float rc = fmaf(-alpha, LD(F.v + c), LD(F.r + c));
+            const float z = rc * LD(F.rd + c);
+            F.r[c] = rc;
+            F.s[c] = z;
+            a3[0] = fmaf(rc, rc, a3[0]);
+            a3[1] = fmaf(rc, z, a3[1]);
+        }
+        tm.template sumf<2>(a3);
+        const float rn = sqrtf(a3[0]);
+        res.iterations = it + 1;
+        res.finalRes = rn / r0;
+        if (res.finalRes < tol) { res.converged = 1; return res; }
+        const float beta = a3[1] / (rz + 1e-30f);
+        for (int c = tm.rank(); c < nC; c += tm.size()) F.pv[c] = fmaf(beta, LD(F.pv + c), LD(F.s + c));
+        tm.sync();
+        rz = a3[1];
+    }
+    return res;
+}
+
+// makeSolver semantics: AMG and PCG run the CG family, every other name BiCGSTAB
+template <class T>
+__device__ SolveResF mx_solve(T &tm, const DevMesh &M, DevWork32 &F, int kind, float *x, float scale, int maxIter,
+                              float tol, bool amgSetup) {
+    if (kind == 3) return mx_amg_pcg(tm, M, F, x, scale, maxIter, tol, amgSetup);
+    if (kind == 0) return mx_pcg(tm, M, F, x, scale, maxIter, tol);
+    return mx_bicgstab(tm, M, F, x, scale, maxIter, tol);
+}
+
+// FP64 defect of the normalised pressure-correction system, d = b s - A y,
+// into f.src; returns this thread's share of |d|^2
+template <class T>
+__device__ __noinline__ double mx_p_defect(T &tm, const DevMesh &M, DevWork32 &F, double s) {
+    double rr = 0.0;
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        double ay = (double)LD(F.diag + c) * (double)LD(F.pp + c);
+        for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
+            const int f = M.cfFace[e], oth = M.cfOther[e];
+            if (oth >= 0) ay = fma((double)LD(F.upper + f), (double)LD(F.pp + oth), ay);
+            else ay = fma((double)LD(F.lower + f), (double)LD(F.pp + (-(oth + 1))), ay);
+        }
+        const double d = LD(F.src64 + c) * s - ay;
+        F.src[c] = (float)d;
+        rr = fma(d, d, rr);
+    }
+    return rr;
+}
+
+// ---------------------------------------------------------------------------
+// initial state (SIMPLESolver::initUniform, SIMPLESolver.cpp:23-51)
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ void mx_init(T &tm, const DevMesh &M, DevInst &I) {
+    DevWork32 &F = I.f;
+    const double nu = I.nu, b1 = I.coeff[2], a1 = I.coeff[9];
+    if (I.initMode == 0) {
+        const double U0 = I.init[0], U1 = I.init[1], U2 = I.init[2], p0 = I.init[3], k0 = I.init[4], w0 = I.init[5];
+        for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+            I.ux[c] = U0; I.uy[c] = U1; I.uz[c] = U2; I.p[c] = p0; I.k[c] = k0;
+            F.f1[c] = 1.0f; F.f2[c] = 1.0f; F.pk[c] = 0.0f; F.cdkw[c] = 0.0f; F.smag[c] = 0.0f;
+            const double y = smax(M.wd[c], 1e-20);
+            const double om = smax(60.0 * nu / (b1 * y * y), w0);
+            I.om[c] = om;
+            F.nut[c] = (float)(a1 * k0 / smax(a1 * om, 1e-20));
+        }
+        for (int b = tm.rank(); b < M.nB; b += tm.size()) {
+            I.ubx[b] = U0; I.uby[b] = U1; I.ubz[b] = U2; I.pb[b] = p0; I.kb[b] = k0; I.omb[b] = w0;
+        }
+        tm.sync();
+        phase_bc_u(tm, M, I);
+        phase_bc_p(tm, M, I);
+        phase_bc_k(tm, M, I, false);
+        phase_bc_w(tm, M, I, 0.075, false);  // applyAllBCs uses applyOmegaBC's default beta1
+    } else {
+        for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+            F.nut[c] = (float)I.nut[c]; F.f1[c] = (float)I.f1[c]; F.f2[c] = (float)I.f2[c];
+            F.pk[c] = (float)I.pk[c]; F.cdkw[c] = (float)I.cdkw[c]; F.smag[c] = 0.0f;
+        }
+    }
+    if (!I.solveZ)
+        for (int c = tm.rank(); c < M.nC; c += tm.size()) { F.g[6][c] = 0.0f; F.g[7][c] = 0.0f; F.g[8][c] = 0.0f; }
+    tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 polishing stage helpers: the FP64 phases (btm_phases64.cuh) assemble
+// the relaxed system in the FP64 arrays; its defect is taken in FP64 and the
+// matrix is rounded once into the FP32 correction system.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __noinline__ double px_defect(T &tm, const DevMesh &M, DevInst &I, const double *x, bool keep64) {
+    DevWork32 &F = I.f;
+    double rr = 0.0;
+    for (int c = tm.rank(); c < M.nC; c += tm.size()) {
+        const double rc = LD(I.src + c) - ldu_row<T>(M, I, x, c);
+        F.src[c] = (float)rc;
+        if (keep64) F.src64[c] = rc;
+        F.diag[c] = (float)LD(I.diag + c);
+        rr = fma(rc, rc, rr);
+    }
+    for (int f = tm.rank(); f < M.nIF; f += tm.size()) {
+        F.upper[f] = (float)LD(I.upper + f);
+        F.lower[f] = (float)LD(I.lower + f);
+    }
+    return rr;
+}
+
+// ---------------------------------------------------------------------------
+// the SIMPLE outer loop in correction form
+//
+// Stage 1 assembles in FP32 (FP32-rounded coefficients: the defect converges
+// to the solution of a slightly perturbed discrete system, and rounding flips
+// of the coefficients put a floor of order 1e-7 under the scaled residuals).
+// Stage 2 ("polish") assembles in FP64 with the FP64 phases, so the final
+// state satisfies the FP64 discrete equations to the reference's convergence
+// test; its correction solves stay FP32.  Stage 2 starts when the largest
+// scaled residual falls below kPolishFactor * tolerance, when stage 1 stops
+// improving, or after three quarters of the iteration cap.  Only stage 2 may
+// declare convergence.
+// ---------------------------------------------------------------------------
+constexpr int kMaxRefine = 2;          // FP64 refinement passes of the pressure correction
+constexpr double kPolishFactor = 100.0;
+constexpr int kStallIters = 3000;      // stage 1 without halving its best residual
+
+template <class T>
+__device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
+    const DevSettings &S = I.S;
+    DevWork32 &F = I.f;
+    const DevGeom32 &G = M.g32;
+    const int nC = M.nC, nB = M.nB;
+    const double nu = I.nu, b1 = I.coeff[2], bstar = I.coeff[8];
+    const float innerTol = (float)S.innerTol;
+    mx_init(tm, M, I);
+    int turbEst = I.initMode == 0 ? 0 : I.turbEstIn;
+    double lastKChange = 1.0, lastOmChange = 1.0;
+    double normUx0 = 1, normUy0 = 1, normP0 = 1;
+    int converged = 0, diverged = 0, finalIter = S.maxIter, ran = 0;
+    int64_t innerMom = 0, innerP = 0, innerTurb = 0, innerRef = 0;
+    double last[6] = {0, 0, 0, 0, 0, 0};
+    const bool turbScheduled = S.turbStart < S.maxIter;
+    const int gradAll = I.solveZ ? 7 : 3;
+    bool polish = false;
+    int polishStart = -1;
+    double bestRes = INFINITY;
+    int bestIter = 0;
+    PhaseClock clk;
+    clk.start(tm.leader());
+    const uint64_t tStart = tm.leader() ? globaltimer_ns() : 0;
+
+    for (int iter = 0; iter < S.maxIter; ++iter) {
+        if (!tm.ok()) break;
+        ran = iter + 1;
+        const bool turbActive = iter >= S.turbStart;
+        const bool turbUpdate = turbActive && ((iter - S.turbStart) % S.turbInterval == 0);
+        // 1. closure fields at the start-of-iteration U
+        if (polish) {
+            phase_velgrad(tm, M, I, 7);
+            phase_grad1(tm, M, I.p, I.pb, I.gpx, I.gpy, I.gpz);
+        } else {
+            mx_velgrad(tm, M, I, gradAll);
+            mx_pgrad(tm, M, I);
+        }
+        tm.sync();
+        if (turbUpdate) {
+            if (!turbEst && iter >= S.turbStart + S.nutFloorIters) turbEst = 1;
+            if (polish) phase_sst(tm, M, I, turbEst ? 0.0 : 0.1 * nu);
+            else mx_sst(tm, M, I, turbEst ? 0.0f : (float)(0.1 * nu));
+            tm.sync();
+        }
+        clk.lap(0);
+        // 2. momentum corrections, component by component with the latest U
+        double eU[3] = {0.0, 0.0, 0.0};
+        for (int comp = 0; comp < 3; ++comp) {
+            if (comp == 2 && !I.solveZ) break;
+            double *u = comp == 0 ? I.ux : (comp == 1 ? I.uy : I.uz);
+            double rr[1];
+            if (polish) {
+                if (comp > 0) {
+                    phase_velgrad(tm, M, I, 1 << (comp - 1));
+                    tm.sync();
+                }
+                phase_mom_faces(tm, M, I, comp);
+                tm.sync();
+                phase_mom_cells(tm, M, I, comp);
+                tm.sync();
+                rr[0] = px_defect(tm, M, I, u, false);
+            } else {
+                if (comp > 0) {
+                    mx_velgrad(tm, M, I, 1 << (comp - 1));
+                    tm.sync();
+                }
+                mx_mom_faces(tm, M, I, comp);
+                tm.sync();
+                rr[0] = mx_mom_cells(tm, M, I, comp);
+            }
+            tm.template sumd<1>(rr);
+            const double en = sqrt(rr[0]);
+            eU[comp] = en;
+            clk.lap(1);
+            const SolveResF rs = mx_solve(tm, M, F, S.momSolver, F.x, en > 0.0 ? (float)(1.0 / en) : 0.0f,
+                                          S.innerIter, innerTol, true);
+            innerMom += rs.iterations;
+            tm.sync();
+            for (int c = tm.rank(); c < nC; c += tm.size()) u[c] = fma((double)F.x[c], en, u[c]);
+            tm.sync();
+            clk.lap(2);
+        }
+        phase_bc_u(tm, M, I);
+        tm.sync();
+        // 3. pressure correction: FP64 continuity defect, FP32 solve, FP64 refinement
+        double pr[1];
+        if (polish) {
+            phase_p_faces(tm, M, I);
+            tm.sync();
+            phase_p_cells(tm, M, I);
+            tm.sync();
+            pr[0] = px_defect(tm, M, I, I.pp, true);
+            for (int c = tm.rank(); c < nC; c += tm.size()) F.aPx[c] = (float)LD(I.aPx + c);
+        } else {
+            mx_p_faces(tm, M, I);
+            tm.sync();
+            pr[0] = mx_p_cells(tm, M, I);
+        }
+        tm.template sumd<1>(pr);
+        const double eP = sqrt(pr[0]);
+        clk.lap(3);
+        if (eP > 0.0) {
+            const double s = 1.0 / eP;
+            const SolveResF rp = mx_solve(tm, M, F, S.pSolver, F.pp, (float)s, S.innerIter, innerTol, true);
+            innerP += rp.iterations;
+            tm.sync();
+            for (int pass = 0; pass < kMaxRefine; ++pass) {
+                double dd[1] = {mx_p_defect(tm, M, F, s)};
+                tm.template sumd<1>(dd);
+                const double dn = sqrt(dd[0]);
+                if (!(dn > S.innerTol)) break;
+                const SolveResF rq = mx_solve(tm, M, F, S.pSolver, F.x, (float)(1.0 / dn), S.innerIter,
+                                              (float)(S.innerTol / dn), false);
+                innerRef += rq.iterations;
+                tm.sync();
+                for (int c = tm.rank(); c < nC; c += tm.size()) F.pp[c] = fmaf(F.x[c], (float)dn, F.pp[c]);
+                tm.sync();
+            }
+            const float pscale = (float)eP;
+            for (int c = tm.rank(); c < nC; c += tm.size()) F.pp[c] *= pscale;
+        } else {
+            for (int c = tm.rank(); c < nC; c += tm.size()) F.pp[c] = 0.0f;
+        }
+        tm.sync();
+        clk.lap(5);
+        for (int b = tm.rank(); b < nB; b += tm.size()) F.ppb[b] = M.bcPp[b] == 0 ? F.pp[M.bown[b]] : 0.0f;
+        tm.sync();
+        // 4. corrections (correctVelocity / correctPressure, SIMPLESolver.cpp:456-475)
+        {
+            const float *P[1] = {F.pp};
+            const float *PB[1] = {F.ppb};
+            const double alphaP = S.alphaP;
+            for (int c = tm.rank(); c < nC; c += tm.size()) {
+                float gx[1], gy[1], gz[1];
+                ggd_cell<T, 1, float>(M, c, P, PB, gx, gy, gz);
+                const float aP = F.aPx[c];
+                const float f = (fabsf(aP) > 1e-30f) ? G.vol[c] / aP : 0.0f;
+                I.ux[c] -= (double)(f * gx[0]);
+                I.uy[c] -= (double)(f * gy[0]);
+                if (I.solveZ) I.uz[c] -= (double)(f * gz[0]);
+                I.p[c] = fma(alphaP, (double)F.pp[c], I.p[c]);
+            }
+            tm.sync();
+            phase_bc_u(tm, M, I);
+            phase_bc_p(tm, M, I);
+            tm.sync();
+        }
+        clk.lap(6);
+        // 5. k and omega corrections
+        if (turbUpdate) {
+            for (int which = 0; which < 2; ++which) {
+                double *phi = which == 0 ? I.k : I.om;
+                double *old = which == 0 ? I.kold : I.omold;
+                const double lo = which == 0 ? S.kMin : S.omegaMin, hi = which == 0 ? S.kMax : 1e15;
+                if (polish && which == 1) {
+                    // The omega wall re-pin leaves a defect that never vanishes in
+                    // the wall cells, so the omega fixed point depends on the
+                    // solver (as in the reference): the polishing stage solves
+                    // omega with the FP64 BiCGSTAB from the old omega, exactly as
+                    // the FP64 engine does.
+                    phase_turb_faces(tm, M, I, which);
+                    tm.sync();
+                    phase_turb_cells(tm, M, I, which);
+                    for (int c = tm.rank(); c < nC; c += tm.size()) old[c] = phi[c];
+                    tm.sync();
+                    const SolveResult rw = team_bicgstab(tm, M, I, phi, S.innerIter, S.innerTol);
+                    innerTurb += rw.iterations;
+                    tm.sync();
+                    for (int c = tm.rank(); c < nC; c += tm.size()) phi[c] = smax(lo, smin(hi, phi[c]));
+                    tm.sync();
+                } else {
+                    double rr[1];
+                    if (polish) {
+                        phase_turb_faces(tm, M, I, which);
+                        tm.sync();
+                        phase_turb_cells(tm, M, I, which);
+                        tm.sync();
+                        rr[0] = px_defect(tm, M, I, phi, false);
+                    } else {
+                        mx_turb_faces(tm, M, I, which);
+                        tm.sync();
+                        rr[0] = mx_turb_cells(tm, M, I, which);
+                    }
+                    tm.template sumd<1>(rr);
+                    const double en = sqrt(rr[0]);
+                    const SolveResF rs = mx_solve(tm, M, F, S.turbSolver, F.x, en > 0.0 ? (float)(1.0 / en) : 0.0f,
+                                                  S.innerIter, innerTol, true);
+                    innerTurb += rs.iterations;
+                    tm.sync();
+                    for (int c = tm.rank(); c < nC; c += tm.size()) {
+                        const double v0 = phi[c];
+                        old[c] = v0;
+                        phi[c] = smax(lo, smin(hi, fma((double)F.x[c], en, v0)));
+                    }
+                    tm.sync();
+                }
+                if (which == 0) phase_bc_k(tm, M, I, true);
+                else phase_bc_w(tm, M, I, b1, true);
+                tm.sync();
+            }
+            // wall re-pin (SIMPLESolver.cpp:884-908) and change norms (:910-922)
+            float mx[4] = {1e-30f, 1e-30f, 0.0f, 0.0f};
+            const double sbs = sqrt(bstar);
+            for (int c = tm.rank(); c < nC; c += tm.size()) {
+                const int b = M.pinFace[c];
+                double omc = I.om[c];
+                if (b >= 0) {
+                    const double y1 = M.bdeltaW[b];
+                    const double omRes = 60.0 * nu / (b1 * y1 * y1);
+                    if (S.useWallFn) {
+                        const double uTau = sqrt(sbs * smax(I.k[c], 1e-30));
+                        const double omLog = uTau / (sbs * S.vonKarman * y1);
+                        omc = sqrt(omRes * omRes + omLog * omLog);
+                    } else {
+                        omc = omRes;
+                    }
+                    I.om[c] = omc;
+                }
+                const double kc = I.k[c];
+                mx[0] = smaxf(mx[0], (float)fabs(kc));
+                mx[1] = smaxf(mx[1], (float)fabs(omc));
+                mx[2] = smaxf(mx[2], (float)fabs(kc - I.kold[c]));
+                mx[3] = smaxf(mx[3], (float)fabs(omc - I.omold[c]));
+            }
+            tm.template maxf<4>(mx);
+            lastKChange = (double)mx[2] / (double)mx[0];
+            lastOmChange = (double)mx[3] / (double)mx[1];
+        }
+        clk.lap(7);
+        // 6. residual bookkeeping, convergence and divergence tests (as the FP64 engine)
+        const double eUx = eU[0], eUy = eU[1], eUz = eU[2];
+        const double eK = turbActive ? lastKChange : 0.0, eW = turbActive ? lastOmChange : 0.0;
+        last[0] = eUx; last[1] = eUy; last[2] = eUz; last[3] = eP; last[4] = eK; last[5] = eW;
+        if (tm.leader() && I.hist && iter < I.histCap)
+            for (int q = 0; q < 6; ++q) I.hist[6 * (size_t)iter + q] = last[q];
+        if (iter == 0) {
+            normUx0 = smax(eUx, 1e-30);
+            normUy0 = smax(eUy, 1e-30);
+            normP0 = smax(eP, 1e-30);
+        } else if (iter < 50) {
+            normP0 = smax(normP0, eP);
+        }
+        const double normMom0 = smax(normUx0, normUy0);
+        const double nUx = normMom0 < 1e-20 ? 0.0 : eUx / normMom0;
+        const double nUy = normMom0 < 1e-20 ? 0.0 : eUy / normMom0;
+        const double nP = normP0 < 1e-20 ? 0.0 : eP / normP0;
+        double maxRes = smax(smax(nUx, nUy), nP);
+        if (turbActive) maxRes = smax(smax(maxRes, lastKChange), lastOmChange);
+        if (!isfinite(eUx) || !isfinite(eUy) || !isfinite(eUz) || !isfinite(eP) || !isfinite(eK) ||
+            !isfinite(eW) || !isfinite(lastKChange) || !isfinite(lastOmChange))
+            maxRes = INFINITY;
+        const bool settled = !turbScheduled || (turbActive && turbEst);
+        if (polish && maxRes < S.convTol && iter > 0 && settled) {
+            converged = 1;
+            finalIter = iter;
+            break;
+        }
+        if (isnan(maxRes) || isinf(maxRes) || maxRes > S.divLimit) {
+            diverged = 1;
+            finalIter = iter;
+            break;
+        }
+        if (!polish) {
+            if (maxRes < 0.5 * bestRes) {
+                bestRes = maxRes;
+                bestIter = iter;
+            }
+            const bool low = settled && maxRes < kPolishFactor * S.convTol;
+            const bool stalled = settled && iter - bestIter > kStallIters;
+            if (low || stalled || 4 * (iter + 1) >= 3 * S.maxIter) {
+                // closure fields continue in FP64 from the FP32 stage's values
+                for (int c = tm.rank(); c < nC; c += tm.size()) {
+                    I.nut[c] = F.nut[c]; I.f1[c] = F.f1[c]; I.f2[c] = F.f2[c]; I.pk[c] = F.pk[c];
+                    I.cdkw[c] = F.cdkw[c]; I.smag[c] = F.smag[c];
+                }
+                tm.sync();
+                polish = true;
+                polishStart = iter + 1;
+            }
+        }
+    }
+    tm.sync();
+    if (!polish) {
+        // closure fields back to the FP64 output arrays
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            I.nut[c] = F.nut[c]; I.f1[c] = F.f1[c]; I.f2[c] = F.f2[c]; I.pk[c] = F.pk[c]; I.cdkw[c] = F.cdkw[c];
+        }
+        tm.sync();
+    }
+    if (tm.leader()) {
+        const bool aborted = !tm.ok();
+        I.out[0] = aborted ? 4 : (diverged ? 2 : (converged ? 0 : 1));
+        I.out[1] = converged;
+        I.out[2] = diverged;
+        I.out[3] = finalIter;
+        I.out[4] = ran;
+        I.out[5] = turbEst;
+        I.out[6] = aborted ? 1 : 0;
+        I.out[7] = polishStart;
+        I.outInner[0] = innerMom + innerP + innerTurb + innerRef;
+        I.outInner[1] = innerMom;
+        I.outInner[2] = innerP;
+        I.outInner[3] = innerTurb;
+        I.outInner[4] = innerRef;
+        for (int q = 0; q < 6; ++q) I.outLast[q] = last[q];
+        for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
+        I.outTime[8] = tStart;
+        I.outTime[9] = globaltimer_ns();
+    }
+}
+
+// One CTA per instance (instances up to the block-mode size limit).
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_mixed_block(DevInst *insts, int n) {
+    __shared__ double red[2 * 32 * kRedSlots];
+    __shared__ DevMesh sM;
+    __shared__ DevInst sI;
+    if (blockIdx.x >= n) return;
+    if (threadIdx.x == 0) {
+        sI = insts[blockIdx.x];
+        sM = *sI.M;
+    }
+    __syncthreads();
+    BlockTeam tm{red, 0};
+    mixed_solve(tm, sM, sI);
+}
+template __global__ void k_mixed_block<256>(DevInst *, int);
+template __global__ void k_mixed_block<512>(DevInst *, int);
+
+int mixed_launch_block(DevInst *dInsts, int n, int threads, void *stream) {
+    if (n <= 0) return 0;
+    if (threads == 256)
+        k_mixed_block<256><<<n, 256, 0, (cudaStream_t)stream>>>(dInsts, n);
+    else
+        k_mixed_block<512><<<n, 512, 0, (cudaStream_t)stream>>>(dInsts, n);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace btm

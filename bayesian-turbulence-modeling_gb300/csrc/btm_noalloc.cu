@@ -130,6 +130,8 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
                                  btm_state *out, btm_history *hist) {
     if (!C || !coeffs) return fail(BTM_ERR_ARG, "null argument");
     if (int e = btm_host::ensure_device()) return e;
+    if (C->settings.precision != BTM_PREC_FP64)
+        return fail(BTM_ERR_ARG, "btm_solve_noalloc runs the FP64 engine only; set precision to fp64");
     if (C->nC > btm_host::block_max_cells())
         return fail(BTM_ERR_ARG, "btm_solve_noalloc: meshes above " + std::to_string(btm_host::block_max_cells()) +
                                      " cells need the cooperative launch; use btm_solve");
@@ -183,12 +185,12 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     int le = btm::engine_launch_block(dI, 1, btm_host::block_threads_for(C->nC), st);
     if (le) return fail(BTM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
     int32_t outv[8] = {0};
-    int64_t innerv = 0;
+    int64_t innerv[5] = {0, 0, 0, 0, 0};
     int32_t errv = 0;
     double lastv[6] = {0};
-    uint64_t tns[8] = {0};
+    uint64_t tns[10] = {0};
     bool ok = ck(cudaMemcpyAsync(outv, I.out, sizeof outv, cudaMemcpyDeviceToHost, st), "status") &&
-              ck(cudaMemcpyAsync(&innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost, st), "status") &&
+              ck(cudaMemcpyAsync(innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost, st), "status") &&
               ck(cudaMemcpyAsync(lastv, I.outLast, sizeof lastv, cudaMemcpyDeviceToHost, st), "status") &&
               ck(cudaMemcpyAsync(tns, I.outTime, sizeof tns, cudaMemcpyDeviceToHost, st), "status") &&
               ck(cudaMemcpyAsync(&errv, I.err, sizeof errv, cudaMemcpyDeviceToHost, st), "status");
@@ -223,9 +225,13 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
         hist->diverged = outv[2];
         hist->final_iter = outv[3];
         hist->iterations_run = outv[4];
-        hist->inner_iterations = innerv;
+        hist->inner_iterations = innerv[0];
+        for (int q = 0; q < 4; ++q) hist->inner_split[q] = innerv[q + 1];
+        hist->polish_start = outv[7];
         for (int q = 0; q < 6; ++q) hist->last_residual[q] = lastv[q];
         for (int q = 0; q < 8; ++q) hist->phase_ms[q] = 1e-6 * (double)tns[q];
+        hist->solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
+        hist->finish_ms = hist->solve_ms;
     }
     if (errv) return fail(BTM_ERR_TIMEOUT, "a bounded device wait timed out; the solve was abandoned");
     return BTM_OK;

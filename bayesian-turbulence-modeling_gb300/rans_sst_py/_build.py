@@ -1,13 +1,14 @@
 """In-tree build of libbtm_gb300.so (CUDA engine + C++ host driver, C ABI).
 
-Compiles csrc/btm_engine.cu and csrc/btm_host.cpp with nvcc for sm_103a only
-(-gencode arch=compute_103a,code=sm_103a), the two translation units in
-parallel, and links them into <package>/_build/libbtm_gb300.so.  A stamp of
-the source contents skips the rebuild when nothing changed.
+Compiles the translation units in csrc/ with nvcc for sm_103a only
+(-gencode arch=compute_103a,code=sm_103a), in parallel, and links them into
+<package>/_build/libbtm_gb300.so.  A stamp of the source contents skips the
+rebuild when nothing changed.
 
-The engine is compiled with -fmad=false: every multiply-add stays two IEEE
-operations so that assembly, gradients and mat-vecs round exactly like the
-reference's face loops.
+The FP64 engine (btm_engine.cu) is compiled with -fmad=false: every
+multiply-add stays two IEEE operations so that assembly, gradients and
+mat-vecs round exactly like the reference's face loops.  The mixed-precision
+engine (btm_mixed.cu) keeps contraction on.
 """
 from __future__ import annotations
 
@@ -23,8 +24,8 @@ BUILD = os.path.join(PKG_ROOT, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 LIB_NAME = "libbtm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["btm_engine.cu", "btm_host.cpp", "btm_noalloc.cu"]
-HEADERS = ["btm_common.h", "btm_host_internal.h"]
+SOURCES = ["btm_engine.cu", "btm_mixed.cu", "btm_host.cpp", "btm_noalloc.cu"]
+HEADERS = ["btm_common.h", "btm_host_internal.h", "btm_team.cuh", "btm_bc.cuh", "btm_phases64.cuh"]
 
 
 def nvcc() -> str:
@@ -67,6 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         [cc] + common + ["-x", "cu", "-c", os.path.join(CSRC, "btm_host.cpp"), "-o",
                          os.path.join(BUILD, "btm_host.o")],
         [cc] + common + ["-c", os.path.join(CSRC, "btm_noalloc.cu"), "-o", os.path.join(BUILD, "btm_noalloc.o")],
+        [cc] + common + ["-c", os.path.join(CSRC, "btm_mixed.cu"), "-o", os.path.join(BUILD, "btm_mixed.o")],
     ]
 
     def run(cmd):
@@ -76,12 +78,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose:
             print(r.stdout + r.stderr)
 
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(run, jobs))
     tmp = out + ".tmp"
     run([cc] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "btm_engine.o"),
                        os.path.join(BUILD, "btm_host.o"), os.path.join(BUILD, "btm_noalloc.o"),
-                       "-cudart", "static"])
+                       os.path.join(BUILD, "btm_mixed.o"), "-cudart", "static"])
     os.replace(tmp, out)
     with open(stamp_file, "w") as fh:
         fh.write(stamp)

@@ -45,6 +45,10 @@ class SolveOutput:
         self.inner_iterations = int(hist.inner_iterations)
         self.last_residual = list(hist.last_residual)
         self.phase_ms = list(hist.phase_ms)
+        self.solve_ms = float(hist.solve_ms)
+        self.finish_ms = float(hist.finish_ms)
+        self.inner_split = list(hist.inner_split)
+        self.polish_start = int(hist.polish_start)
         self.residuals = residuals
 
 

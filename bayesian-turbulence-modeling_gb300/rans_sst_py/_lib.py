@@ -46,7 +46,7 @@ class BtmSettings(C.Structure):
                 ("omega_min", C.c_double), ("use_wall_functions", C.c_int32),
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
-                ("turbulence_solver", C.c_int32)]
+                ("turbulence_solver", C.c_int32), ("precision", C.c_int32)]
 
 
 class BtmState(C.Structure):
@@ -63,10 +63,13 @@ class BtmHistory(C.Structure):
     _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
                 ("final_iter", C.c_int32), ("iterations_run", C.c_int32),
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
-                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8)]
+                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8),
+                ("solve_ms", C.c_double), ("finish_ms", C.c_double), ("inner_split", C.c_int64 * 4),
+                ("polish_start", C.c_int32)]
 
 
 SOLVER_CODES = {"PCG": 0, "BiCGSTAB": 1, "GaussSeidel": 2, "AMG": 3}
+PRECISION_CODES = {"fp64": 0, "mixed": 1}
 PHASES = {"grad": 1, "sst": 2, "momentum": 3, "pressure": 4, "k": 5, "omega": 6, "spmv": 7,
           "bicgstab": 8, "amgpcg": 9, "pcg": 11}
 
@@ -200,6 +203,10 @@ def settings_struct(s) -> BtmSettings:
     st.pressure_solver = SOLVER_CODES.get(s.pressure_solver, 1)
     st.momentum_solver = SOLVER_CODES.get(s.momentum_solver, 1)
     st.turbulence_solver = SOLVER_CODES.get(s.turbulence_solver, 1)
+    prec = getattr(s, "precision", "fp64")
+    if prec not in PRECISION_CODES:
+        raise ValueError(f"precision must be one of {sorted(PRECISION_CODES)}, not {prec!r}")
+    st.precision = PRECISION_CODES[prec]
     return st
 
 

@@ -182,7 +182,9 @@ class InferenceParameterSet:
 class SolverSettings:
     """SolverSettings (core/include/FlowFields.hpp:53-132) with the snake_case
     attribute names of Bindings.cpp:414-441.  pressure_solver /
-    momentum_solver / turbulence_solver are also settable here."""
+    momentum_solver / turbulence_solver are also settable here, and
+    `precision` ("fp64", the reference's arithmetic, or "mixed": FP32 bulk
+    with FP64 state, defects and refinement) selects the device engine."""
 
     def __init__(self):
         self.max_iterations = 500
@@ -213,6 +215,7 @@ class SolverSettings:
         self.von_karman = 0.41
         self.wall_fn_E = 9.0
         self.sst_variant = 0
+        self.precision = "fp64"
 
     def copy(self) -> "SolverSettings":
         s = SolverSettings()

@@ -51,6 +51,7 @@ MAX_ITER, TOL = 60000, 1e-8
 INIT = dict(u=(20.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
 CPU_SAMPLE_ITERS = 1500
 WORKLOAD = "theta256_channel4x128_re550"
+PRECISION = "fp64"
 
 
 def make_case_inputs():
@@ -63,6 +64,7 @@ def make_case_inputs():
     s.body_force = rs.Vec3(1.0, 0.0, 0.0)
     s.max_iterations = MAX_ITER
     s.convergence_tol = TOL
+    s.precision = PRECISION
     return m, bcs, 1.0 / RE_TAU, s
 
 
@@ -344,7 +346,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="one launch of 304 instances capped at 200 outer iterations (for ncu captures)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
+    global PRECISION
+    PRECISION = args.precision
     world, rank, local = dist_setup()
     if args.profile_case:
         run_profile_case()

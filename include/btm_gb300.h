@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BTM_ABI_VERSION 1
+#define BTM_ABI_VERSION 2
 
 /* ---- status codes -------------------------------------------------------- */
 #define BTM_OK              0
@@ -73,6 +73,15 @@ extern "C" {
 #define BTM_LS_BICGSTAB     1
 #define BTM_LS_GAUSSSEIDEL  2
 #define BTM_LS_AMG          3
+
+/* ---- arithmetic of a solve ------------------------------------------------
+ * FP64: the reference's arithmetic throughout (the drop-in).
+ * MIXED: FP32 assembly, closure, gradients, Krylov and AMG work; FP64 flow
+ * state, equation defects, continuity defect and pressure-correction
+ * refinement, so a converged solve satisfies the FP64 discrete equations
+ * built from FP32-rounded coefficients.  No reference counterpart. */
+#define BTM_PREC_FP64       0
+#define BTM_PREC_MIXED      1
 
 /* ---- SST closure variants (core/include/SSTModel.hpp:48) ------------------- */
 #define BTM_SST_FULL        0
@@ -140,6 +149,7 @@ typedef struct btm_settings {
     int32_t pressure_solver;       /* BTM_LS_* */
     int32_t momentum_solver;
     int32_t turbulence_solver;
+    int32_t precision;             /* BTM_PREC_*; not a reference field */
 } btm_settings;
 
 /* Initial state.  mode 0 = cold uniform start exactly as
@@ -181,6 +191,17 @@ typedef struct btm_history {
      * [2] momentum solves, [3] p' assembly, [4] AMG numeric setup,
      * [5] p' solve, [6] corrections + BCs, [7] k/omega assembly+solves */
     double  phase_ms[8];
+    /* device time of this instance from the start of its solve to its end,
+     * and its end relative to the earliest instance start of the same
+     * launch (the latency of a request submitted with the batch) */
+    double  solve_ms;
+    double  finish_ms;
+    /* inner iterations by system: momentum, pressure correction, k and
+     * omega, FP64 refinement passes of the pressure correction */
+    int64_t inner_split[4];
+    /* mixed precision: first outer iteration of the FP64-assembly polishing
+     * stage (-1: FP64 engine, or the stage never started) */
+    int32_t polish_start;
 } btm_history;
 
 typedef struct btm_case btm_case;

@@ -41,7 +41,7 @@ class Settings(C.Structure):
                 ("omega_min", C.c_double), ("use_wall_functions", C.c_int32),
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
-                ("turbulence_solver", C.c_int32)]
+                ("turbulence_solver", C.c_int32), ("precision", C.c_int32)]
 
 
 class State(C.Structure):
@@ -58,7 +58,9 @@ class History(C.Structure):
     _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
                 ("final_iter", C.c_int32), ("iterations_run", C.c_int32),
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
-                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8)]
+                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8),
+                ("solve_ms", C.c_double), ("finish_ms", C.c_double), ("inner_split", C.c_int64 * 4),
+                ("polish_start", C.c_int32)]
 
 
 CELL_FIELDS = ("p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw")

@@ -1,0 +1,127 @@
+"""Mixed-precision engine (precision = "mixed"): FP32 assembly, closure,
+gradients, Krylov and AMG work around an FP64 flow state, FP64 equation
+defects and an FP64-refined pressure correction.
+
+The error bar is 1e-6 relative L2 against the FP64 reference solution (the
+reference's converged and stagnated fields stored in tests/golden), for U, k,
+omega and nu_t; pressure is compared against the dynamic pressure scale
+(periodic domains fix p only up to a near-constant level).
+"""
+import json
+
+import numpy as np
+import pytest
+
+import cases
+from rans_sst_py import FlowBoundaryConditions, SolverSettings, Vec3, Case, solve, solve_batch
+from rans_sst_py._lib import BtmError
+
+pytestmark = pytest.mark.gpu
+
+COEFF = cases.COEFF_DEFAULTS
+TOL_FIELDS = 1e-6
+
+
+def settings_from(g, tol, cap):
+    d = json.loads(bytes(g["settings"]).decode())
+    s = SolverSettings()
+    for k, v in d.items():
+        setattr(s, k, Vec3(*v) if k == "body_force" else v)
+    s.max_iterations, s.convergence_tol = cap, tol
+    s.precision = "mixed"
+    return s
+
+
+def init_from(g):
+    a = g["init"]
+    return dict(u=tuple(a[:3]), p=float(a[3]), k=float(a[4]), omega=float(a[5]))
+
+
+def mesh_from(g):
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    m.compute_wall_distance()
+    return m
+
+
+def errors(state, g, pre):
+    out = {f: cases.rel_l2(state[f], g[f"{pre}_{f}"]) for f in ("U", "k", "omega", "nuT")}
+    U = g[f"{pre}_U"]
+    q = 0.5 * np.max(np.sum(U * U, axis=1))
+    out["p"] = float(np.linalg.norm(state["p"] - g[f"{pre}_p"]) / (q * np.sqrt(len(U))))
+    return out
+
+
+def _check(errs, tol=TOL_FIELDS):
+    for f, e in errs.items():
+        assert e <= tol, (f, e, errs)
+
+
+@pytest.mark.parametrize("name", ["chan180_4x32", "couette_4x32"])
+def test_mixed_converged_matches_fp64_reference(name):
+    """Cold start to the 1e-8 scaled residual in mixed precision; the converged
+    fields agree with the reference's stagnated FP64 solution within 1e-6."""
+    g = cases.load_golden(name)
+    m = mesh_from(g)
+    bcs = (FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0) if name.startswith("chan")
+           else cases.couette_case(4, 32)[1])
+    case = Case(m, bcs, float(g["nu"]), settings_from(g, 1e-8, 4 * int(g["conv_iterations_run"])))
+    out = solve(case, COEFF, 0, init_from(g))
+    assert out.converged
+    _check(errors(out.state, g, "stag"))
+
+
+def test_mixed_duct3d_stagnation():
+    """3-D duct (z-momentum active), fixed iteration count as the golden."""
+    g = cases.load_golden("duct_4x16x16")
+    m = mesh_from(g)
+    case = Case(m, FlowBoundaryConditions.channel_defaults(m, 0, 0, 0), float(g["nu"]),
+                settings_from(g, 0.0, int(g["stag_iterations_run"])))
+    out = solve(case, COEFF, 0, init_from(g))
+    _check(errors(out.state, g, "stag"))
+
+
+def test_mixed_batch_matches_solo_bitwise():
+    """A mixed instance gives bit-identical results alone and inside a batch
+    with FP64 and mixed instances of other meshes."""
+    m1, b1, nu1, i1 = cases.periodic_channel(32, 180.0)
+    m2, b2, nu2, i2 = cases.couette_case(4, 16)
+    s1 = cases.channel_settings(300, 0.0)
+    s1.precision = "mixed"
+    s2 = cases.couette_settings(300, 0.0)
+    c1 = Case(m1, b1, nu1, s1)
+    c2 = Case(m2, b2, nu2, s2)
+    th = np.array(COEFF)
+    th2 = th.copy()
+    th2[9] *= 1.1
+    solo = solve(c1, th2, 0, i1)
+    batch = solve_batch([c2, c1, c1, c2], [th, th2, th, th2], None, [i2, i1, i1, i2])
+    for f in ("U", "p", "k", "omega", "nuT"):
+        assert np.array_equal(solo.state[f], batch[1].state[f]), f
+
+
+def test_mixed_warm_start_from_neighbouring_theta():
+    """Warm start from the converged state of a nearby theta (the warm-start
+    cache use): fewer iterations than a cold solve, same converged fields."""
+    m, bcs, nu, init = cases.periodic_channel(32, 180.0)
+    s = cases.channel_settings(40000, 1e-8)
+    s.precision = "mixed"
+    case = Case(m, bcs, nu, s)
+    th = np.array(COEFF)
+    th2 = th.copy()
+    th2[9] *= 1.02
+    first = solve(case, th, 0, init)
+    warm = solve(case, th2, 0, first.state)
+    cold = solve(case, th2, 0, init)
+    assert first.converged and warm.converged and cold.converged
+    assert warm.iterations_run < cold.iterations_run
+    for f in ("U", "k", "omega", "nuT"):
+        assert cases.rel_l2(warm.state[f], cold.state[f]) <= TOL_FIELDS, f
+
+
+def test_mixed_rejects_grid_sized_mesh():
+    m, bcs, nu, init = cases.periodic_channel(512, 180.0, nx=34, ratio=1.01)   # 17408 cells
+    s = cases.channel_settings(1, 0.0)
+    s.precision = "mixed"
+    case = Case(m, bcs, nu, s)
+    with pytest.raises(BtmError, match="mixed precision"):
+        solve(case, COEFF, 0, init)
