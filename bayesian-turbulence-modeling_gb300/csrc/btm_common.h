@@ -2,6 +2,7 @@
 // device engine (btm_engine.cu).  Plain structs of device pointers; one
 // DevMesh per case (read-only after creation), one DevInst per solve instance.
 #pragma once
+#include <stddef.h>
 #include <stdint.h>
 
 namespace btm {
@@ -162,6 +163,7 @@ int engine_grid_blocks(int *blocks_out);
 int engine_launch_debug(DevInst *dInst, void *stream);
 
 // mixed-precision engine entry points (btm_mixed.cu)
-int mixed_launch_block(DevInst *dInsts, int n, int threads, void *stream);
+size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN);
+int mixed_launch_block(DevInst *dInsts, int n, int threads, size_t smemBytes, void *stream);
 
 }  // namespace btm

@@ -964,9 +964,15 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             }
             if (!mixIdx.empty()) {
                 int maxCells = 0;
-                for (int i : mixIdx) maxCells = std::max(maxCells, jobs[i].C->nC);
+                size_t smem = 0;
+                for (int i : mixIdx) {
+                    const btm_case *Cm = jobs[i].C;
+                    maxCells = std::max(maxCells, Cm->nC);
+                    smem = std::max(smem, btm::mixed_smem_bytes(Cm->nC, Cm->nIF, Cm->amgVecTotal, Cm->amgValTotal,
+                                                                Cm->dmesh.coarseDirect ? Cm->amgCoarseN : 1));
+                }
                 int e = btm::mixed_launch_block(dInsts + blockIdx.size(), (int)mixIdx.size(),
-                                                block_threads_for(maxCells), st);
+                                                block_threads_for(maxCells), smem, st);
                 if (e) throw BtmError(BTM_ERR_CUDA, std::string("mixed launch: ") + cudaGetErrorString((cudaError_t)e));
             }
         } else {

@@ -727,28 +727,46 @@ __device__ __noinline__ void mx_amg_gs_sweep(T &tm, const DevMesh &M, DevWork32 
     }
 }
 
+// residual of level l restricted into level l+1 in one pass (x_{l+1} = 0):
+// each coarse row sums b - A x over its aggregate's members, and every fine
+// row belongs to exactly one aggregate
+// one damped-Jacobi sweep on a coarse level (l >= 1): reads x, writes `out`
+// (the V-cycle ping-pongs between the level's x and r arrays)
+constexpr float kJacobiWeight = 0.7f;
+template <class T>
+__device__ __noinline__ void mx_amg_jacobi(T &tm, const DevMesh &M, DevWork32 &F, int l, const float *x, float *out) {
+    const AmgLevelDev &L = M.lev[l];
+    const float *b = lev_bf(F, M, l);
+    const float *val = lev_valsf(F, M, l);
+    const float *rd = lev_rdf(F, M, l);
+    for (int i = tm.rank(); i < L.n; i += tm.size()) {
+        float s = LD(b + i);
+        for (int k = L.rowPtr[i]; k < L.rowPtr[i + 1]; ++k) s = fmaf(-LD(val + k), LD(x + L.colIdx[k]), s);
+        out[i] = fmaf(kJacobiWeight * LD(rd + i), s, LD(x + i));
+    }
+    tm.sync();
+}
+
 template <class T>
 __device__ __noinline__ void mx_amg_restrict(T &tm, const DevMesh &M, DevWork32 &F, int l) {
     const AmgLevelDev &L = M.lev[l];
     const float *x = lev_xf(F, M, l), *b = lev_bf(F, M, l), *val = lev_valsf(F, M, l);
-    float *r = lev_rf(F, M, l);
-    for (int i = tm.rank(); i < L.n; i += tm.size()) {
-        float s;
-        if (l == 0) {
-            s = ldu_rowf<T>(M, F, x, i);
-        } else {
-            s = 0.0f;
-            for (int q = L.rowPtr[i]; q < L.rowPtr[i + 1]; ++q) s = fmaf(LD(val + q), LD(x + L.colIdx[q]), s);
-        }
-        r[i] = LD(b + i) - s;
-    }
-    tm.sync();
     const AmgLevelDev &C = M.lev[l + 1];
     float *bc = lev_bf(F, M, l + 1), *xc = lev_xf(F, M, l + 1);
     for (int J = tm.rank(); J < C.n; J += tm.size()) {
-        float s = 0.0f;
-        for (int q = L.aggOff[J]; q < L.aggOff[J + 1]; ++q) s += LD(r + L.aggMem[q]);
-        bc[J] = s;
+        float acc = 0.0f;
+        for (int q = L.aggOff[J]; q < L.aggOff[J + 1]; ++q) {
+            const int i = L.aggMem[q];
+            float s;
+            if (l == 0) {
+                s = ldu_rowf<T>(M, F, x, i);
+            } else {
+                s = 0.0f;
+                for (int k = L.rowPtr[i]; k < L.rowPtr[i + 1]; ++k) s = fmaf(LD(val + k), LD(x + L.colIdx[k]), s);
+            }
+            acc += LD(b + i) - s;
+        }
+        bc[J] = acc;
         xc[J] = 0.0f;
     }
     tm.sync();
@@ -781,33 +799,69 @@ __device__ void mx_amg_coarse_solve(T &tm, const DevMesh &M, DevWork32 &F) {
     }
 }
 
+// numeric Galerkin values and reciprocal diagonals of levels [l0, nLevels)
 template <class T>
-__device__ void mx_amg_setup(T &tm, const DevMesh &M, DevWork32 &F) {
-    mx_amg_level_rd(tm, M, F, 0);
-    for (int l = 1; l < M.nLevels; ++l) {
-        mx_amg_galerkin(tm, M, F, l);
-        tm.sync();
+__device__ void mx_amg_values_from(T &tm, const DevMesh &M, DevWork32 &F, int l0) {
+    for (int l = l0; l < M.nLevels; ++l) {
+        if (l > 0) {
+            mx_amg_galerkin(tm, M, F, l);
+            tm.sync();
+        }
         mx_amg_level_rd(tm, M, F, l);
     }
     tm.sync();
-    if (M.coarseDirect) mx_amg_coarse_inverse(tm, M, F);
 }
 
-// symmetric V-cycle: 2 pre-sweeps (colours ascending), 2 post (descending)
+// symmetric V-cycle on levels [l0, nLevels): 2 pre-sweeps (colours
+// ascending), 2 post-sweeps (colours descending)
+// two smoothing sweeps of level l: multicolour Gauss-Seidel on level 0
+// (colours ascending before the coarse correction, descending after), a pair
+// of damped-Jacobi sweeps (x -> r -> x) on coarser levels
 template <class T>
-__device__ void mx_amg_vcycle(T &tm, const DevMesh &M, DevWork32 &F) {
+__device__ void mx_amg_smooth2(T &tm, const DevMesh &M, DevWork32 &F, int l, bool post) {
+    if (l == 0) {
+        mx_amg_gs_sweep(tm, M, F, 0, post);
+        mx_amg_gs_sweep(tm, M, F, 0, post);
+    } else {
+        float *x = lev_xf(F, M, l), *tmp = lev_rf(F, M, l);
+        mx_amg_jacobi(tm, M, F, l, x, tmp);
+        mx_amg_jacobi(tm, M, F, l, tmp, x);
+    }
+}
+
+template <class T>
+__device__ void mx_amg_vcycle_from(T &tm, const DevMesh &M, DevWork32 &F, int l0) {
     const int nl = M.nLevels;
-    for (int l = 0; l < nl - 1; ++l) {
-        mx_amg_gs_sweep(tm, M, F, l, false);
-        mx_amg_gs_sweep(tm, M, F, l, false);
+    for (int l = l0; l < nl - 1; ++l) {
+        mx_amg_smooth2(tm, M, F, l, false);
         mx_amg_restrict(tm, M, F, l);
     }
     mx_amg_coarse_solve(tm, M, F);
-    for (int l = nl - 2; l >= 0; --l) {
+    for (int l = nl - 2; l >= l0; --l) {
         mx_amg_prolong(tm, M, F, l);
-        mx_amg_gs_sweep(tm, M, F, l, true);
-        mx_amg_gs_sweep(tm, M, F, l, true);
+        mx_amg_smooth2(tm, M, F, l, true);
     }
+}
+
+// Coarse levels (values, reciprocal diagonals, the coarsest inverse) are
+// refreshed when `coarse` is set and otherwise kept from an earlier outer
+// iteration: a Galerkin hierarchy of an earlier SPD pressure matrix is still
+// an SPD preconditioner for the current one, and level 0 always smooths with
+// the current matrix.  Every level runs on the whole team: on the coarse
+// levels a single warp's dependent latency chain cost more than the barriers
+// it saved.
+template <class T>
+__device__ void mx_amg_setup(T &tm, const DevMesh &M, DevWork32 &F, bool coarse = true) {
+    mx_amg_level_rd(tm, M, F, 0);
+    tm.sync();
+    if (!coarse) return;
+    mx_amg_values_from(tm, M, F, 1);
+    if (M.coarseDirect) mx_amg_coarse_inverse(tm, M, F);
+}
+
+template <class T>
+__device__ void mx_amg_vcycle(T &tm, const DevMesh &M, DevWork32 &F) {
+    mx_amg_vcycle_from(tm, M, F, 0);
 }
 
 // AMG-preconditioned CG (AMGSolver::solve, LinearSolver.hpp:602-653):
@@ -1027,14 +1081,17 @@ __device__ __noinline__ double px_defect(T &tm, const DevMesh &M, DevInst &I, co
 // of the coefficients put a floor of order 1e-7 under the scaled residuals).
 // Stage 2 ("polish") assembles in FP64 with the FP64 phases, so the final
 // state satisfies the FP64 discrete equations to the reference's convergence
-// test; its correction solves stay FP32.  Stage 2 starts when the largest
-// scaled residual falls below kPolishFactor * tolerance, when stage 1 stops
-// improving, or after three quarters of the iteration cap.  Only stage 2 may
+// test; its correction solves stay FP32 (except omega, see below).  Stage 2
+// starts when the largest scaled residual falls below kPolishFactor *
+// tolerance, when stage 1 stops improving close to the tolerance (its FP32
+// floor), or after three quarters of the iteration cap.  Only stage 2 may
 // declare convergence.
 // ---------------------------------------------------------------------------
 constexpr int kMaxRefine = 2;          // FP64 refinement passes of the pressure correction
 constexpr double kPolishFactor = 100.0;
-constexpr int kStallIters = 3000;      // stage 1 without halving its best residual
+constexpr int kStallIters = 3000;      // stage 1 without halving its best residual ...
+constexpr double kStallBand = 1e4;     // ... while within this factor of the tolerance
+constexpr int kAmgRefresh = 8;         // outer iterations between coarse-hierarchy refreshes
 
 template <class T>
 __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
@@ -1055,6 +1112,7 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     const int gradAll = I.solveZ ? 7 : 3;
     bool polish = false;
     int polishStart = -1;
+    int amgAge = 0;
     double bestRes = INFINITY;
     int bestIter = 0;
     PhaseClock clk;
@@ -1140,7 +1198,13 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         clk.lap(3);
         if (eP > 0.0) {
             const double s = 1.0 / eP;
-            const SolveResF rp = mx_solve(tm, M, F, S.pSolver, F.pp, (float)s, S.innerIter, innerTol, true);
+            if (S.pSolver == 3) {
+                // a hierarchy shared with AMG solves of other systems is rebuilt every time
+                mx_amg_setup(tm, M, F, amgAge == 0 || S.momSolver == 3 || S.turbSolver == 3);
+                amgAge = amgAge + 1 == kAmgRefresh ? 0 : amgAge + 1;
+                clk.lap(4);
+            }
+            const SolveResF rp = mx_solve(tm, M, F, S.pSolver, F.pp, (float)s, S.innerIter, innerTol, false);
             innerP += rp.iterations;
             tm.sync();
             for (int pass = 0; pass < kMaxRefine; ++pass) {
@@ -1305,7 +1369,7 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
                 bestIter = iter;
             }
             const bool low = settled && maxRes < kPolishFactor * S.convTol;
-            const bool stalled = settled && iter - bestIter > kStallIters;
+            const bool stalled = settled && iter - bestIter > kStallIters && maxRes < kStallBand * S.convTol;
             if (low || stalled || 4 * (iter + 1) >= 3 * S.maxIter) {
                 // closure fields continue in FP64 from the FP32 stage's values
                 for (int c = tm.rank(); c < nC; c += tm.size()) {
@@ -1348,30 +1412,148 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Shared-memory staging of one instance's solver working set.
+//
+// The Krylov and multigrid vectors and the LDU coefficients are rewritten in
+// every barrier-separated phase, mostly by other threads than the ones that
+// read them next; from global memory each such read is an L2 round trip.
+// Placed in the CTA's dynamic shared memory they stay on chip.  Arrays keep
+// their meaning and only change address (generic pointers), so the phase code
+// is unchanged; they are placed in order of how often an outer iteration
+// touches them, each one if it still fits.  The host sizes the buffer with
+// mixed_smem_bytes (same order, same alignment).
+// ---------------------------------------------------------------------------
+constexpr int kSmemAlign = 16;
+struct SmemCopy {
+    void *dst;
+    const void *src;
+    int bytes;
+};
+
+__device__ __host__ inline size_t smem_round(size_t b) { return (b + kSmemAlign - 1) & ~size_t(kSmemAlign - 1); }
+
+// sizes in placement order (bytes); returns the count
+__device__ __host__ inline int smem_items(int nC, int nIF, int64_t vec, int64_t val, int nc, int nGather, size_t *sz) {
+    int q = 0;
+    sz[q++] = 4 * ((size_t)nC + 2 * (size_t)nIF);                  // diag | upper | lower
+    for (int i = 0; i < 7; ++i) sz[q++] = 4 * (size_t)nC;           // r s t pv v pp x
+    sz[q++] = 4 * ((size_t)nC + (size_t)vec);                       // amgRd
+    for (int i = 0; i < 3; ++i) sz[q++] = 4 * (size_t)(vec > 0 ? vec : 1);   // amgX amgB amgR
+    sz[q++] = 4 * (size_t)(val > 0 ? val : 1);                      // amgVal
+    for (int i = 0; i < 5; ++i) sz[q++] = 4 * (size_t)nC;           // rh ph sh rd src
+    sz[q++] = 4 * (size_t)nc * nc;                                  // coarse inverse
+    sz[q++] = 4 * ((size_t)nC + 1);                                 // cfOff
+    sz[q++] = 4 * (size_t)nGather;                                  // cfFace
+    sz[q++] = 4 * (size_t)nGather;                                  // cfOther
+    return q;
+}
+
+__device__ void stage_smem(DevMesh &M, DevInst &I, unsigned char *dsm, size_t cap, SmemCopy *copies, int *nCopies) {
+    DevWork32 &F = I.f;
+    const int nC = M.nC, nIF = M.nIF;
+    const int nc = M.coarseDirect ? M.lev[M.nLevels - 1].n : 1;
+    const int nGather = 2 * nIF;
+    size_t sz[32];
+    const int nItems = smem_items(nC, nIF, M.amgVecTotal, M.amgValTotal, nc, nGather, sz);
+    size_t off = 0;
+    int nc_ = 0;
+    for (int q = 0; q < nItems; ++q) {
+        const size_t b = smem_round(sz[q]);
+        if (off + b > cap) continue;
+        void *p = dsm + off;
+        off += b;
+        float *f = (float *)p;
+        switch (q) {
+            case 0: F.diag = f; F.upper = f + nC; F.lower = f + nC + nIF; break;
+            case 1: F.r = f; break;
+            case 2: F.s = f; break;
+            case 3: F.t = f; break;
+            case 4: F.pv = f; break;
+            case 5: F.v = f; break;
+            case 6: F.pp = f; break;
+            case 7: F.x = f; break;
+            case 8: F.amgRd = f; break;
+            case 9: F.amgX = f; break;
+            case 10: F.amgB = f; break;
+            case 11: F.amgR = f; break;
+            case 12: F.amgVal = f; break;
+            case 13: F.rh = f; break;
+            case 14: F.ph = f; break;
+            case 15: F.sh = f; break;
+            case 16: F.rd = f; break;
+            case 17: F.src = f; break;
+            case 18: F.ainv = f; break;
+            case 19: copies[nc_++] = {p, M.cfOff, (int)sz[q]}; M.cfOff = (const int32_t *)p; break;
+            case 20: copies[nc_++] = {p, M.cfFace, (int)sz[q]}; M.cfFace = (const int32_t *)p; break;
+            case 21: copies[nc_++] = {p, M.cfOther, (int)sz[q]}; M.cfOther = (const int32_t *)p; break;
+        }
+    }
+    *nCopies = nc_;
+}
+
 // One CTA per instance (instances up to the block-mode size limit).
 template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_mixed_block(DevInst *insts, int n) {
+__global__ void __launch_bounds__(NT, 512 / NT) k_mixed_block(DevInst *insts, int n, int smemBytes) {
+    extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ double red[2 * 32 * kRedSlots];
     __shared__ DevMesh sM;
     __shared__ DevInst sI;
+    __shared__ SmemCopy copies[4];
+    __shared__ int nCopies;
     if (blockIdx.x >= n) return;
     if (threadIdx.x == 0) {
         sI = insts[blockIdx.x];
         sM = *sI.M;
+        nCopies = 0;
+        if (smemBytes > 0) stage_smem(sM, sI, dsm, (size_t)smemBytes, copies, &nCopies);
+    }
+    __syncthreads();
+    for (int q = 0; q < nCopies; ++q) {
+        const int words = copies[q].bytes / 4;
+        const int32_t *src = (const int32_t *)copies[q].src;
+        int32_t *dst = (int32_t *)copies[q].dst;
+        for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
     BlockTeam tm{red, 0};
     mixed_solve(tm, sM, sI);
 }
-template __global__ void k_mixed_block<256>(DevInst *, int);
-template __global__ void k_mixed_block<512>(DevInst *, int);
+template __global__ void k_mixed_block<256>(DevInst *, int, int);
+template __global__ void k_mixed_block<512>(DevInst *, int, int);
 
-int mixed_launch_block(DevInst *dInsts, int n, int threads, void *stream) {
+// dynamic shared memory that would hold an instance's whole solver working set
+size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN) {
+    size_t sz[32];
+    const int n = smem_items(nC, nIF, vecTotal, valTotal, coarseN, 2 * nIF, sz);
+    size_t t = 0;
+    for (int q = 0; q < n; ++q) t += smem_round(sz[q]);
+    return t;
+}
+
+// Launch with `smemBytes` of dynamic shared memory per CTA, capped at what
+// leaves the CTAs-per-SM of the launch bounds resident.
+int mixed_launch_block(DevInst *dInsts, int n, int threads, size_t smemBytes, void *stream) {
     if (n <= 0) return 0;
-    if (threads == 256)
-        k_mixed_block<256><<<n, 256, 0, (cudaStream_t)stream>>>(dInsts, n);
-    else
-        k_mixed_block<512><<<n, 512, 0, (cudaStream_t)stream>>>(dInsts, n);
+    int dev = 0, perSm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e != cudaSuccess) return (int)e;
+    const int ctas = 512 / threads;
+    // static shared memory of the kernel plus the per-CTA reservation
+    const size_t reserve = 8 * 1024;
+    size_t cap = (size_t)perSm / ctas > reserve ? (size_t)perSm / ctas - reserve : 0;
+    if (smemBytes > cap) smemBytes = cap;
+    smemBytes &= ~size_t(kSmemAlign - 1);
+    if (threads == 256) {
+        e = cudaFuncSetAttribute(k_mixed_block<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
+        if (e != cudaSuccess) return (int)e;
+        k_mixed_block<256><<<n, 256, smemBytes, (cudaStream_t)stream>>>(dInsts, n, (int)smemBytes);
+    } else {
+        e = cudaFuncSetAttribute(k_mixed_block<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
+        if (e != cudaSuccess) return (int)e;
+        k_mixed_block<512><<<n, 512, smemBytes, (cudaStream_t)stream>>>(dInsts, n, (int)smemBytes);
+    }
     return (int)cudaGetLastError();
 }
 

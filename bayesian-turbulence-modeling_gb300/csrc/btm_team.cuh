@@ -80,10 +80,13 @@ struct BlockTeam {
         buf ^= 1;
     }
 
-    // FP32 sums whose cross-warp part is accumulated in FP64: every warp
-    // reduces its lanes in FP32, then lane 0 of every warp folds the per-warp
-    // partials in FP64 in a fixed order and broadcasts to its warp.  All
-    // threads receive identical totals; FP64 work is per warp, not per thread.
+    // FP32 sums (Krylov dot products of the mixed-precision engine): a warp
+    // butterfly, then every warp re-reduces the per-warp partials with the
+    // same butterfly, so all threads hold identical totals after one barrier.
+    // The fold stays in FP32: on GB300 a chain of dependent FP64 additions per
+    // reduction doubled the BiCGSTAB time, and pairwise FP32 summation of at
+    // most 16k products is accurate to ~1e-6, far inside what the Krylov
+    // scalars need (the equation defects themselves are FP64).
     template <int N>
     __device__ __forceinline__ void sumf(float *v) {
 #pragma unroll
@@ -91,21 +94,18 @@ struct BlockTeam {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        double *rb = red + buf * 32 * kRedSlots;
+        float *rb = reinterpret_cast<float *>(red + buf * 32 * kRedSlots);   // [slot][warp]
         if (lane == 0)
 #pragma unroll
-            for (int j = 0; j < N; ++j) rb[warp * kRedSlots + j] = (double)v[j];
+            for (int j = 0; j < N; ++j) rb[j * 32 + warp] = v[j];
         __syncthreads();
         const int nw = blockDim.x >> 5;
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            float t = 0.0f;
-            if (lane == 0) {
-                double s = 0.0;
-                for (int q = 0; q < nw; ++q) s += rb[q * kRedSlots + j];
-                t = (float)s;
-            }
-            v[j] = __shfl_sync(0xffffffffu, t, 0);
+            float s = lane < nw ? rb[j * 32 + lane] : 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            v[j] = s;
         }
         buf ^= 1;
     }

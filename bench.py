@@ -10,19 +10,24 @@ Workload (the batched-theta configuration on the plane-channel case):
     draws with kappa outside [0.35, 0.5] are InvalidParameters and are served
     without a solve, exactly as the reference's ForwardModel::evaluate does;
   * every valid theta: a cold SIMPLE solve to the reference's 1e-8 scaled
-    residual (max 60000 outer iterations), FP64.
+    residual (max 60000 outer iterations) in the batched mixed-precision form
+    (FP32 bulk around an FP64 state, FP64 polishing stage; --precision fp64
+    times the plain FP64 drop-in instead).
 One step = the whole 256-theta batch in one persistent launch.
 
 `value` is converged solves / device time of the launch (CUDA events on the
 launching stream, inputs resident).  `e2e` is the same metric through the
 public batched API (rans_sst_py.solve_batch) with host buffers: parameters
 in, every instance's full flow state copied back to the host each step.
-The working set (~110 MB of device state for 222 instances) fits in L2.
+`latency_ms` gives p50/p99 of the per-instance completion times inside the
+launch.  After the timed steps the same batch runs once through the plain
+FP64 engine: `fp64_plain` is its throughput and `error_vs_fp64` the
+per-instance relative L2 of the mixed-precision fields against it.
 
 `--impl reference` times the CPU restatement of the reference algorithm
 (oracle/, or the reference built from its sources when present) on all host
 cores: a bounded sample of outer iterations per process, converted to solves/s
-with the measured iterations-per-converged-solve of the GPU run.
+with the measured iterations-per-converged-solve of the GPU FP64 path.
 """
 from __future__ import annotations
 
@@ -51,7 +56,7 @@ MAX_ITER, TOL = 60000, 1e-8
 INIT = dict(u=(20.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
 CPU_SAMPLE_ITERS = 1500
 WORKLOAD = "theta256_channel4x128_re550"
-PRECISION = "fp64"
+PRECISION = "mixed"
 
 
 def make_case_inputs():
@@ -137,9 +142,20 @@ class ClockSampler:
 # (~376 B: two LDU mat-vecs and 29 vector streams, the BiCGStab figure).
 BYTES_PER_CELL_OUTER = 1100.0
 BYTES_PER_CELL_INNER = 376.0
+# Mixed precision: FP32 coefficient, gradient and closure streams plus the
+# FP64 state and defect streams (~760 B per cell per outer iteration), FP32
+# Krylov iterations (2 LDU mat-vecs at 44 B + 29 FP32 streams = 204 B).
+BYTES_PER_CELL_OUTER_MIXED = 760.0
+BYTES_PER_CELL_INNER_MIXED = 204.0
+# ncu DRAM bytes (read + write) per cell-iteration of the profile case (304
+# instances x 200 outer iterations of the 4x128 channel), per engine.
+TRAFFIC_PER_CELL_ITER = {"fp64": 460.0, "mixed": 55.0}
+FIXED_POINT_SUBSET = 8
 
 
-def algorithmic_bytes(n_cells, outer, inner):
+def algorithmic_bytes(n_cells, outer, inner, mixed=False):
+    if mixed:
+        return n_cells * (BYTES_PER_CELL_OUTER_MIXED * outer + BYTES_PER_CELL_INNER_MIXED * inner)
     return n_cells * (BYTES_PER_CELL_OUTER * outer + BYTES_PER_CELL_INNER * inner)
 
 
@@ -239,6 +255,26 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def _batch_stats(outs):
+    conv = sum(o.converged for o in outs)
+    fin = np.array([o.finish_ms for o in outs])
+    return conv, fin
+
+
+def _field_errors(a_outs, b_outs):
+    """Per-instance relative L2 of a against b (U, k, omega, nu_t), and the
+    pressure against the dynamic pressure scale."""
+    errs = {f: [] for f in ("U", "k", "omega", "nuT", "p")}
+    for a, b in zip(a_outs, b_outs):
+        for f in ("U", "k", "omega", "nuT"):
+            errs[f].append(float(np.linalg.norm(a.state[f] - b.state[f]) / max(np.linalg.norm(b.state[f]), 1e-300)))
+        U = b.state["U"]
+        q = 0.5 * np.max(np.sum(U * U, axis=1))
+        errs["p"].append(float(np.linalg.norm(a.state["p"] - b.state["p"]) / (q * np.sqrt(len(U)))))
+    return {f: {"max": max(v), "p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99))}
+            for f, v in errs.items()}
+
+
 def run_gpu(args, world, rank, local):
     import rans_sst_py as rs
     from rans_sst_py._lib import lib
@@ -258,21 +294,23 @@ def run_gpu(args, world, rank, local):
     # parameters go in, every instance's full flow state comes back.  The
     # device time of the persistent launch inside the call (CUDA events on
     # its stream) gives `value`; the wall time of the whole call gives `e2e`.
-    def step():
+    def step(c=case):
         t0 = time.perf_counter()
-        outs = rs.solve_batch(cases, cf, None, inits, want_state=True)
+        outs = rs.solve_batch([c] * n, cf, None, inits, want_state=True)
         return outs, lib().btm_last_launch_ms(), time.perf_counter() - t0
 
     for _ in range(args.warmup):
         step()
     dist_barrier(world)
-    dev_ms, wall_s, conv_counts, outer, inner = [], [], [], 0, 0
+    dev_ms, wall_s, conv_counts, outer, inner, fins = [], [], [], 0, 0, []
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             outs, ms, wall = step()
             dev_ms.append(ms)
             wall_s.append(wall)
-            conv_counts.append(sum(o.converged for o in outs))
+            conv, fin = _batch_stats(outs)
+            conv_counts.append(conv)
+            fins.append(fin)
             outer += sum(o.iterations_run for o in outs)
             inner += sum(o.inner_iterations for o in outs)
     dist_barrier(world)
@@ -285,32 +323,79 @@ def run_gpu(args, world, rank, local):
     h2d = n * (11 * 8 + 4 + 48)
     nb = m.n_boundary_faces()
     d2h = n * 8 * (m.n_cells() * 11 + nb * 6)
+    fin = np.concatenate(fins)
+    polish = [o.polish_start / max(1, o.iterations_run) for o in outs if o.polish_start >= 0]
 
     iters_per_solve = outer / max(1, args.steps * n)
-    bytes_per_launch = algorithmic_bytes(m.n_cells(), outer / args.steps, inner / args.steps)
+    mixed = PRECISION == "mixed"
+    bytes_per_launch = algorithmic_bytes(m.n_cells(), outer / args.steps, inner / args.steps, mixed)
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch / step_s / 1e9
+    cell_iters = m.n_cells() * outer / args.steps
+    traffic = (TRAFFIC_PER_CELL_ITER[PRECISION] * cell_iters) if args.traffic is None else args.traffic
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": args.traffic, "peak_kind": peak_kind,
-                "note": "algorithmic bytes of the persistent solve kernel; the working set is L2-resident and "
-                        "the kernel is bound by the FP64 pipe (GB300 FP64 is 1/64 of FP32)"}
+                "traffic": traffic, "peak_kind": peak_kind,
+                "note": "algorithmic bytes of the persistent solve kernel over its CUDA-event time; the "
+                        "per-instance working set lives in L2 / shared memory, so the kernel is bound by "
+                        "barrier-separated phase latency and the FP64 pipe, not by HBM; traffic = ncu DRAM "
+                        "bytes per cell-iteration of the profile case scaled to this launch"}
     line = {"metric": "converged RANS solves/sec", "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_theta": N_THETA, "n_valid": int(n), "cells": m.n_cells(),
-                       "tol": TOL, "converged_per_step": converged, "iters_per_converged_solve": iters_per_solve,
-                       "inner_iters_per_outer": inner / max(1, outer), "l2": "working set L2-resident; "
-                       "no flush needed for a single persistent launch per step"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": PRECISION, "n_theta": N_THETA, "n_valid": int(n),
+                       "cells": m.n_cells(), "tol": TOL, "converged_per_step": converged,
+                       "iters_per_converged_solve": iters_per_solve,
+                       "inner_iters_per_outer": inner / max(1, outer),
+                       "polish_start_frac": statistics.mean(polish) if polish else None,
+                       "l2": "working set L2/shared-memory resident; no flush needed for a single persistent "
+                             "launch per step"},
+            "latency_ms": {"p50": float(np.percentile(fin, 50)), "p99": float(np.percentile(fin, 99)),
+                           "max": float(fin.max()),
+                           "note": "per-instance device time from the launch's first instance start to the "
+                                   "instance's end"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps, "clocks": clk, "roofline": roofline}
+    fp64_iters = None
+    if rank == 0 and mixed and not args.no_fp64_compare:
+        # the plain FP64 drop-in on the same batch (one launch, untimed by the
+        # bench clock): its throughput, and the per-instance field error of the
+        # mixed-precision results against it
+        s64 = s.copy()
+        s64.precision = "fp64"
+        case64 = rs.Case(m, bcs, nu, s64)
+        outs64, ms64, _ = step(case64)
+        conv64, fin64 = _batch_stats(outs64)
+        fp64_iters = sum(o.iterations_run for o in outs64) / n
+        line["fp64_plain"] = {"value": conv64 / (ms64 / 1e3), "unit": "solves/s", "ms": ms64,
+                              "converged": conv64, "iters_per_converged_solve": fp64_iters,
+                              "latency_ms": {"p50": float(np.percentile(fin64, 50)),
+                                             "p99": float(np.percentile(fin64, 99))},
+                              "speedup_of_mixed": value / (conv64 / (ms64 / 1e3))}
+        line["error_vs_fp64"] = _field_errors(outs, outs64)
+        line["error_vs_fp64"]["note"] = ("both engines stopped at the 1e-8 scaled residual; slowly converging "
+                                        "instances stop ~1e-6 from their fixed point on either path")
+        # precision error proper: a subset converged to 1e-11 in both engines
+        sub = list(range(0, n, max(1, n // FIXED_POINT_SUBSET)))[:FIXED_POINT_SUBSET]
+        tight = {}
+        for prec in ("mixed", "fp64"):
+            st = s.copy()
+            st.precision, st.convergence_tol, st.max_iterations = prec, 1e-11, 100000
+            ct = rs.Case(m, bcs, nu, st)
+            tight[prec] = rs.solve_batch([ct] * len(sub), cf[sub], None, [INIT] * len(sub), want_state=True)
+        fp = _field_errors(tight["mixed"], tight["fp64"])
+        fp["instances"] = len(sub)
+        fp["converged"] = [sum(o.converged for o in tight[p]) for p in ("mixed", "fp64")]
+        fp["note"] = "mixed vs FP64, both converged to the 1e-11 scaled residual (fixed-point error)"
+        line["error_fixed_point"] = fp
     if rank == 0 and not args.no_cpu_baseline:
         n_proc = os.cpu_count() or 1
         it_rate, _, wall_cpu = cpu_sample(n_proc, CPU_SAMPLE_ITERS)
-        line["cpu_baseline"] = {"value": it_rate / iters_per_solve, "unit": "solves/s", "cores": n_proc,
+        ips = fp64_iters or iters_per_solve
+        line["cpu_baseline"] = {"value": it_rate / ips, "unit": "solves/s", "cores": n_proc,
                                 "kind": reference_kind(),
                                 "sample": f"{n_proc} processes x {CPU_SAMPLE_ITERS} outer iterations of the "
-                                          f"4x128 channel ({wall_cpu:.1f} s wall), converted with the GPU run's "
-                                          f"{iters_per_solve:.0f} iterations per converged solve (extrapolated)"}
+                                          f"4x128 channel ({wall_cpu:.1f} s wall), converted with "
+                                          f"{ips:.0f} outer iterations per converged FP64 solve (extrapolated)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -331,7 +416,8 @@ def run_profile_case():
     inner = sum(o.inner_iterations for o in outs)
     ms = lib().btm_last_launch_ms()
     print(json.dumps({"profile_case": True, "instances": len(cf), "outer_iterations": it, "inner_iterations": inner,
-                      "launch_ms": ms, "bytes_algorithmic": algorithmic_bytes(m.n_cells(), it, inner)}))
+                      "launch_ms": ms, "precision": PRECISION,
+                      "bytes_algorithmic": algorithmic_bytes(m.n_cells(), it, inner, PRECISION == "mixed")}))
 
 
 def main():
@@ -341,12 +427,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch, if measured")
-    ap.add_argument("--iters-per-solve", type=float, default=30681.0,
-                    help="reference arm: outer iterations per converged solve of the 4x128 channel")
+    ap.add_argument("--iters-per-solve", type=float, default=18128.0,
+                    help="reference arm: mean outer iterations per converged FP64 solve of the batch "
+                         "(measured on the GPU FP64 path of the same 219 theta)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="one launch of 304 instances capped at 200 outer iterations (for ncu captures)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="engine of the timed arm (mixed: the batched mixed-precision form)")
+    ap.add_argument("--no-fp64-compare", action="store_true",
+                    help="skip the plain-FP64 launch of the same batch and the error report")
     args = ap.parse_args()
     global PRECISION
     PRECISION = args.precision

@@ -5,6 +5,7 @@ reference sources exist:
 
     make -C oracle ref
     python tests/golden/make_golden.py [case ...]
+    python tests/golden/make_golden.py bfs_perm_1920+cont   # add the continuation run
 
 Each .npz holds the exact mesh (MSH1 bytes), the case inputs (nu, settings as
 JSON, initial state) and the reference outputs.  Stagnation states are the
@@ -119,6 +120,28 @@ def make_bfs():
     return out
 
 
+def add_bfs_continuation():
+    """Extend bfs_perm_1920.npz (keeping its expensive converged run) with the
+    reference continued for 200 outer iterations from its converged state
+    (warm start, convergence test off): the comparator for the device
+    engines started from the same state."""
+    path = os.path.join(HERE, "bfs_perm_1920.npz")
+    g = dict(np.load(path))
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    m.compute_wall_distance()
+    nu = float(g["nu"])
+    init = dict(u=tuple(g["init"][:3]), p=float(g["init"][3]), k=float(g["init"][4]), omega=float(g["init"][5]))
+    from rans_sst_py import FlowBoundaryConditions
+    bcs = FlowBoundaryConditions.bfs_defaults(m, 1.0, init["k"], init["omega"])
+    s = cases.bfs_settings(200, 0.0)
+    warm = {f: g[f"conv_{f}"] for f in FIELDS}
+    warm["turb_established"] = int(g["conv_turb_established"])
+    a, info, res = ref_solve(bytes(g["mesh"]), m, bcs, nu, s, dict(warm=warm), residual_capacity=200)
+    pack("cont200", a, info, g)
+    g["cont200_residuals"] = res[:info["iterations_run"]]
+    return g
+
+
 def make_couette():
     m, bcs, nu, init = cases.couette_case()
     s = cases.couette_settings(30000, 1e-8)
@@ -198,6 +221,8 @@ def make_units():
 
 MAKERS = {"units": make_units, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
           "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1}
+# makers that extend an existing file instead of producing a new case
+EXTENDERS = {"bfs_perm_1920": add_bfs_continuation}
 
 
 def main(names):
@@ -205,7 +230,11 @@ def main(names):
         raise SystemExit("reference driver not built: make -C oracle ref")
     for name in names or list(MAKERS):
         t0 = time.time()
-        out = MAKERS[name]()
+        if name.endswith("+cont"):
+            name = name[:-5]
+            out = EXTENDERS[name]()
+        else:
+            out = MAKERS[name]()
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **out)
         print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB in {time.time() - t0:.0f} s", flush=True)

@@ -142,6 +142,21 @@ def test_bfs_short_pin(oracle):
             assert_same(st[f], g[f"pin{n}_{f}"], 0.0 if SAME_PLATFORM else 1e-12)
 
 
+def test_bfs_continuation_pin(oracle):
+    """200 iterations warm-started from the reference's converged BFS state."""
+    g = cases.load_golden("bfs_perm_1920")
+    m = mesh_from(g)
+    s = settings_from(g)
+    s.max_iterations, s.convergence_tol = 200, 0.0
+    ini = init_from(g)
+    bcs = FlowBoundaryConditions.bfs_defaults(m, 1.0, ini["k"], ini["omega"])
+    warm = {f: g[f"conv_{f}"] for f in FIELDS}
+    warm["turb_established"] = int(g["conv_turb_established"])
+    st, h = oracle.solve(m, bcs, float(g["nu"]), s, cases.COEFF_DEFAULTS, 0, warm=warm)
+    for f in FIELDS:
+        assert_same(st[f], g[f"cont200_{f}"], 0.0 if SAME_PLATFORM else 1e-12)
+
+
 def test_duct_short_pin(oracle):
     g = cases.load_golden("duct_4x16x16")
     m = mesh_from(g)
