@@ -144,15 +144,20 @@ struct DevInst {
     int32_t *out;           // [8]: status, converged, diverged, finalIter, itersRun, turbEst, _, _
     int64_t *outInner;      // [5] inner iterations: total, momentum, pressure, turbulence, refinement
     uint64_t *outTime;      // [10] ns per phase [0..7] (leader thread's globaltimer), solve start [8] and end [9]
-    double *outLast;        // [6] last residual entry
+    double *outLast;        // [6] last residual entry, [6..8] the residual scales used
     double *hist;           // [histCap*6] or null
     int32_t histCap;
     int32_t turbEstIn;      // turbEstablished of a warm state
+    int32_t normFixed;      // 1: scale residuals by normIn instead of this solve's first defects
+    double normIn[3];       // momentum x, momentum y, continuity scales of an earlier cold solve
     // debug phase I/O (test hooks)
     int32_t dbgPhase, dbgArg;
     double *dbgIn, *dbgOut;
     // mixed-precision bulk (null for the FP64 engine)
     DevWork32 f;
+    // served requests: completion flag in mapped host memory (null otherwise),
+    // set by the leader after every output is written
+    volatile int32_t *doneFlag;
 };
 
 // engine entry points (btm_engine.cu)

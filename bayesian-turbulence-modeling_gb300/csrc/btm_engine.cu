@@ -612,7 +612,11 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
         last[0] = eUx; last[1] = eUy; last[2] = eUz; last[3] = eP; last[4] = eK; last[5] = eW;
         if (tm.leader() && I.hist && iter < I.histCap)
             for (int q = 0; q < 6; ++q) I.hist[6 * (size_t)iter + q] = last[q];
-        if (iter == 0) {
+        if (I.normFixed) {
+            normUx0 = I.normIn[0];
+            normUy0 = I.normIn[1];
+            normP0 = I.normIn[2];
+        } else if (iter == 0) {
             normUx0 = smax(eUx, 1e-30);
             normUy0 = smax(eUy, 1e-30);
             normP0 = smax(eP, 1e-30);
@@ -657,9 +661,16 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
         I.outInner[3] = innerTurb;
         I.outInner[4] = 0;
         for (int q = 0; q < 6; ++q) I.outLast[q] = last[q];
+        I.outLast[6] = normUx0;
+        I.outLast[7] = normUy0;
+        I.outLast[8] = normP0;
         for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
         I.outTime[8] = tStart;
         I.outTime[9] = globaltimer_ns();
+        if (I.doneFlag) {
+            __threadfence_system();
+            *I.doneFlag = 1;
+        }
     }
 }
 

@@ -730,6 +730,7 @@ void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, 
         I.turbEstIn = ws->turb_established;
     }
     I.solveZ = zeroZ ? 0 : 1;
+    I.normFixed = 0;
 }
 
 // host staging for SoA <-> AoS conversion
@@ -1159,4 +1160,14 @@ void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, 
 }
 int block_max_cells() { return ::block_max_cells(); }
 int block_threads_for(int maxCells) { return ::block_threads_for(maxCells); }
+void make_slab(btm_case *C, Slab &S) { ::make_slab(C, S); }
+void ensure_mixed(btm_case *C, Slab &S) { ::ensure_mixed(C, S); }
+void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
+                  std::vector<double> &stage) {
+    ::upload_state(C, I, ws, st, stage);
+}
+void download_state(btm_case *C, const btm::DevInst &I, btm_state *o, cudaStream_t st,
+                    std::vector<double> &stage) {
+    ::download_state(C, I, o, st, stage);
+}
 }  // namespace btm_host

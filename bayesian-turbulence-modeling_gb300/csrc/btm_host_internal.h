@@ -46,4 +46,12 @@ void set_error(const std::string &msg);
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init);
 int block_max_cells();
 int block_threads_for(int maxCells);
+// instance slab (FP64 fields and work) and its FP32 bulk for the mixed engine
+void make_slab(btm_case *C, Slab &S);
+void ensure_mixed(btm_case *C, Slab &S);
+// FP64 state between a caller's btm_state and a slab (synchronises `st`)
+void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
+                  std::vector<double> &stage);
+void download_state(btm_case *C, const btm::DevInst &I, btm_state *o, cudaStream_t st,
+                    std::vector<double> &stage);
 }  // namespace btm_host

@@ -1083,14 +1083,15 @@ __device__ __noinline__ double px_defect(T &tm, const DevMesh &M, DevInst &I, co
 // state satisfies the FP64 discrete equations to the reference's convergence
 // test; its correction solves stay FP32 (except omega, see below).  Stage 2
 // starts when the largest scaled residual falls below kPolishFactor *
-// tolerance, when stage 1 stops improving close to the tolerance (its FP32
-// floor), or after three quarters of the iteration cap.  Only stage 2 may
-// declare convergence.
+// tolerance, when a window of stage-1 iterations no longer improves it by 10 %
+// (its FP32 floor: a warm start normalises by a small first defect, so the
+// floor can lie far above the tolerance), or after three quarters of the
+// iteration cap.  Only stage 2 may declare convergence.
 // ---------------------------------------------------------------------------
 constexpr int kMaxRefine = 2;          // FP64 refinement passes of the pressure correction
 constexpr double kPolishFactor = 100.0;
-constexpr int kStallIters = 3000;      // stage 1 without halving its best residual ...
-constexpr double kStallBand = 1e4;     // ... while within this factor of the tolerance
+constexpr int kStallWindow = 2000;     // stage 1 stalls when a window of this many iterations ...
+constexpr double kStallGain = 0.9;     // ... does not push its best residual below this times the last one
 constexpr int kAmgRefresh = 8;         // outer iterations between coarse-hierarchy refreshes
 
 template <class T>
@@ -1113,8 +1114,8 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     bool polish = false;
     int polishStart = -1;
     int amgAge = 0;
-    double bestRes = INFINITY;
-    int bestIter = 0;
+    double bestRes = INFINITY, winBest = INFINITY;
+    int winStart = 0;
     PhaseClock clk;
     clk.start(tm.leader());
     const uint64_t tStart = tm.leader() ? globaltimer_ns() : 0;
@@ -1336,7 +1337,11 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         last[0] = eUx; last[1] = eUy; last[2] = eUz; last[3] = eP; last[4] = eK; last[5] = eW;
         if (tm.leader() && I.hist && iter < I.histCap)
             for (int q = 0; q < 6; ++q) I.hist[6 * (size_t)iter + q] = last[q];
-        if (iter == 0) {
+        if (I.normFixed) {
+            normUx0 = I.normIn[0];
+            normUy0 = I.normIn[1];
+            normP0 = I.normIn[2];
+        } else if (iter == 0) {
             normUx0 = smax(eUx, 1e-30);
             normUy0 = smax(eUy, 1e-30);
             normP0 = smax(eP, 1e-30);
@@ -1364,12 +1369,15 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
             break;
         }
         if (!polish) {
-            if (maxRes < 0.5 * bestRes) {
-                bestRes = maxRes;
-                bestIter = iter;
+            winBest = smin(winBest, maxRes);
+            bool stalled = false;
+            if (iter + 1 - winStart >= kStallWindow) {
+                stalled = settled && !(winBest < kStallGain * bestRes);
+                bestRes = smin(bestRes, winBest);
+                winBest = INFINITY;
+                winStart = iter + 1;
             }
             const bool low = settled && maxRes < kPolishFactor * S.convTol;
-            const bool stalled = settled && iter - bestIter > kStallIters && maxRes < kStallBand * S.convTol;
             if (low || stalled || 4 * (iter + 1) >= 3 * S.maxIter) {
                 // closure fields continue in FP64 from the FP32 stage's values
                 for (int c = tm.rank(); c < nC; c += tm.size()) {
@@ -1406,9 +1414,16 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         I.outInner[3] = innerTurb;
         I.outInner[4] = innerRef;
         for (int q = 0; q < 6; ++q) I.outLast[q] = last[q];
+        I.outLast[6] = normUx0;
+        I.outLast[7] = normUy0;
+        I.outLast[8] = normP0;
         for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
         I.outTime[8] = tStart;
         I.outTime[9] = globaltimer_ns();
+        if (I.doneFlag) {
+            __threadfence_system();
+            *I.doneFlag = 1;
+        }
     }
 }
 

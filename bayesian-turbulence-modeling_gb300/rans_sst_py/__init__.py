@@ -16,8 +16,9 @@ from ._types import (BCType, EvaluationResult, EvaluationStatus, FlowBoundaryCon
 from ._observe import ObservationOperator
 from ._forward import ForwardModel, SolveOutput, solve, solve_batch
 from ._lib import Case, BtmError, library_path
+from ._server import Server
 
 __all__ = ["Mesh", "BCType", "EvaluationResult", "EvaluationStatus", "FlowBoundaryConditions",
            "InferenceParameterSet", "PatchBC", "SolverSettings", "SSTCoefficients", "Vec3",
            "ObservationOperator", "ForwardModel", "SolveOutput", "solve", "solve_batch", "Case",
-           "BtmError", "library_path"]
+           "BtmError", "library_path", "Server"]

@@ -24,7 +24,7 @@ BUILD = os.path.join(PKG_ROOT, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 LIB_NAME = "libbtm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["btm_engine.cu", "btm_mixed.cu", "btm_host.cpp", "btm_noalloc.cu"]
+SOURCES = ["btm_engine.cu", "btm_mixed.cu", "btm_host.cpp", "btm_server.cpp", "btm_noalloc.cu"]
 HEADERS = ["btm_common.h", "btm_host_internal.h", "btm_team.cuh", "btm_bc.cuh", "btm_phases64.cuh"]
 
 
@@ -67,6 +67,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
                          os.path.join(BUILD, "btm_engine.o")],
         [cc] + common + ["-x", "cu", "-c", os.path.join(CSRC, "btm_host.cpp"), "-o",
                          os.path.join(BUILD, "btm_host.o")],
+        [cc] + common + ["-x", "cu", "-c", os.path.join(CSRC, "btm_server.cpp"), "-o",
+                         os.path.join(BUILD, "btm_server.o")],
         [cc] + common + ["-c", os.path.join(CSRC, "btm_noalloc.cu"), "-o", os.path.join(BUILD, "btm_noalloc.o")],
         [cc] + common + ["-c", os.path.join(CSRC, "btm_mixed.cu"), "-o", os.path.join(BUILD, "btm_mixed.o")],
     ]
@@ -83,7 +85,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = out + ".tmp"
     run([cc] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "btm_engine.o"),
                        os.path.join(BUILD, "btm_host.o"), os.path.join(BUILD, "btm_noalloc.o"),
-                       os.path.join(BUILD, "btm_mixed.o"), "-cudart", "static"])
+                       os.path.join(BUILD, "btm_mixed.o"), os.path.join(BUILD, "btm_server.o"),
+                       "-cudart", "static"])
     os.replace(tmp, out)
     with open(stamp_file, "w") as fh:
         fh.write(stamp)

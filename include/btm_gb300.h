@@ -40,6 +40,7 @@ extern "C" {
 #define BTM_ERR_NODEVICE   -4   /* no CUDA device visible                         */
 #define BTM_ERR_TIMEOUT    -5   /* a bounded device-side wait ran out             */
 #define BTM_ERR_INTERNAL   -6
+#define BTM_EAGAIN          1   /* server: not admitted now / nothing completed within the timeout */
 
 /* ---- solve outcome: the reference EvaluationStatus
  *      (core/include/EvaluationTypes.hpp:6-12, python/Bindings.cpp:276-281) ---- */
@@ -270,7 +271,60 @@ double btm_last_launch_ms(void);
 #define BTM_PHASE_SPMV          7   /* LinearSystem::matvec                    */
 #define BTM_PHASE_BICGSTAB      8   /* BiCGSTABSolver::solve                   */
 #define BTM_PHASE_AMGPCG        9   /* AMG-preconditioned CG                   */
-#define BTM_PHASE_ITER         10   /* N full SIMPLE outer iterations          */
+#define BTM_PHASE_ITER         10   /* ---- served request loop with continuous batching -------------------------
+ *
+ * No single reference counterpart: it replaces the calibration layer's
+ * pattern of issuing ForwardModel::evaluate calls from many MCMC chains /
+ * design loops (python/parallel_mcmc.py:37-57) with one resident server per
+ * GPU.  Cases (meshes, AMG structure) stay on the device; each request
+ * reserves a solve slot (per-case device slab) when one is free or can be
+ * allocated within the HBM budget, otherwise btm_server_submit returns
+ * BTM_EAGAIN.  Admitted requests are launched in groups by
+ * btm_server_poll / btm_server_flush while earlier groups still run; each
+ * instance signals its own completion (a flag in mapped host memory), so a
+ * slot is recycled as soon as its solve ends, not when its whole group does.
+ * warm_tag >= 0 keeps the request's final state on the device under that tag
+ * and starts the next request carrying the same tag (same case) from it.
+ * Results (state, history) are written into the caller's buffers, which
+ * must stay valid until the request is returned by btm_server_poll. */
+typedef struct btm_server btm_server;
+typedef struct btm_request {
+    int64_t id;                /* caller's request id, returned by poll          */
+    btm_case *c;
+    const double *coeffs;      /* 11 SST constants                               */
+    int32_t variant;
+    const btm_init *init;      /* start when the tag has no state yet (NULL: cold defaults) */
+    int64_t warm_tag;          /* -1: none                                        */
+    btm_state *out;            /* may be NULL                                     */
+    btm_history *hist;         /* may be NULL; residual history not recorded      */
+    int32_t flags;             /* BTM_REQ_*                                       */
+} btm_request;
+
+/* Scale a tag-started solve's residuals by the residual scales of the tag's
+ * first (cold) solve instead of its own first defects.  The reference's
+ * evaluate() normalises a warm start by that start's (small) iteration-0
+ * defects, so a warm start must reduce them by the full tolerance again and
+ * its convergence classification depends on what ran before
+ * (incompressible/src/ForwardModel.cpp:49-56); with this flag a warm solve is
+ * converged when its defects are as small as the chain's cold solve required. */
+#define BTM_REQ_TAG_NORMS 1
+
+/* max_slots: solve slots (concurrent instances) over all cases;
+ * hbm_budget_bytes: device memory the server may hold for slots and tags. */
+int btm_server_create(int32_t max_slots, int64_t hbm_budget_bytes, btm_server **out);
+void btm_server_destroy(btm_server *s);
+/* BTM_OK: admitted (launched at the next poll/flush); BTM_EAGAIN: no slot or
+ * memory free now; negative: error. */
+int btm_server_submit(btm_server *s, const btm_request *r);
+/* launch every admitted request that is not running yet */
+int btm_server_flush(btm_server *s);
+/* Launch pending requests, then wait up to timeout_ms for completions; fills
+ * ids[0..*n_done) (at most cap).  BTM_EAGAIN when nothing completed in time. */
+int btm_server_poll(btm_server *s, int32_t timeout_ms, int64_t *ids, int32_t cap, int32_t *n_done);
+/* counters: slots in use, slots allocated, bytes held, requests in flight */
+int btm_server_stats(const btm_server *s, int32_t *busy_slots, int32_t *slots, int64_t *bytes, int32_t *inflight);
+
+/* N full SIMPLE outer iterations          */
 int btm_debug_phase(btm_case *c, int32_t phase, const double *coeffs,
                     int32_t variant, int32_t arg, const double *in, int64_t n_in,
                     double *out, int64_t n_out);
