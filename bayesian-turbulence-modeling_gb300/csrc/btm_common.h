@@ -54,10 +54,12 @@ struct DevMesh {
     const double *w, *area, *deltaC;              // deltaC = max(delta, 1e-20)
     const double *nx, *ny, *nz, *sfx, *sfy, *sfz; // unit normal, n * area
     const double *ex, *ey, *ez;                   // d / max(delta, 1e-30)
+    const double *aOverD;                         // area / deltaC (FP64-accurate fast assembly)
     // boundary faces [nB] (index b = face - nIF)
     const int32_t *bown;
     const double *barea, *bdeltaC, *bdeltaW;      // bdeltaW = max(delta, 1e-20) for omega wall BC
     const double *bnx, *bny, *bnz, *bsfx, *bsfy, *bsfz;
+    const double *baOverD;                        // barea / bdeltaC
     const int32_t *bwall;                         // face belongs to a 'wall' patch
     const int32_t *bout;                          // face belongs to an 'outlet' patch
     const int32_t *bcU, *bcP, *bcK, *bcW;         // BC codes (BC_*) per face

@@ -550,6 +550,10 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
                  g_barea = P(f32(barea)), g_brdel = P(recip32(bdC, 0.0, 0.0)), g_bnx = P(f32(bnx)),
                  g_bny = P(f32(bny)), g_bnz = P(f32(bnz)), g_vol = P(f32(vol)), g_rvol = P(recip32(vol, 1e-30, 1.0)),
                  g_wd = P(f32(wd));
+    std::vector<double> aOverD(nIF), baOverD(nB);
+    for (int f = 0; f < nIF; ++f) aOverD[f] = area[f] / dC[f];
+    for (int b = 0; b < nB; ++b) baOverD[b] = barea[b] / bdC[b];
+    const size_t o_aod = P(aOverD), o_baod = P(baOverD);
     struct LevOff { size_t rowPtr, colIdx, diagPos, gOff, gIdx, map, aggOff, aggMem, colorOff, colorRows; };
     std::vector<LevOff> lo(nL);
     int64_t valTot = 0, vecTot = 0;
@@ -589,6 +593,8 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
     D.vol = F64(o_vol); D.wd = F64(o_wd); D.cfOff = I32(o_cfOff); D.cfFace = I32(o_cfFace); D.cfOther = I32(o_cfOther);
     D.cbOff = I32(o_cbOff); D.cbFace = I32(o_cbFace); D.cbpOff = I32(o_cbpOff); D.cbpFace = I32(o_cbpFace);
     D.pinFace = I32(o_pin);
+    D.aOverD = F64(o_aod);
+    D.baOverD = F64(o_baod);
     auto F32 = [&](size_t at) { return (const float *)(base + at); };
     btm::DevGeom32 &G = D.g32;
     G.w = F32(g_w); G.area = F32(g_area); G.rdelta = F32(g_rdel); G.nx = F32(g_nx); G.ny = F32(g_ny);

@@ -1127,8 +1127,8 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         const bool turbUpdate = turbActive && ((iter - S.turbStart) % S.turbInterval == 0);
         // 1. closure fields at the start-of-iteration U
         if (polish) {
-            phase_velgrad(tm, M, I, 7);
-            phase_grad1(tm, M, I.p, I.pb, I.gpx, I.gpy, I.gpz);
+            phase_velgrad<T, true>(tm, M, I, 7);
+            phase_grad1<T, true>(tm, M, I.p, I.pb, I.gpx, I.gpy, I.gpz);
         } else {
             mx_velgrad(tm, M, I, gradAll);
             mx_pgrad(tm, M, I);
@@ -1136,7 +1136,7 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         tm.sync();
         if (turbUpdate) {
             if (!turbEst && iter >= S.turbStart + S.nutFloorIters) turbEst = 1;
-            if (polish) phase_sst(tm, M, I, turbEst ? 0.0 : 0.1 * nu);
+            if (polish) phase_sst<T, true>(tm, M, I, turbEst ? 0.0 : 0.1 * nu);
             else mx_sst(tm, M, I, turbEst ? 0.0f : (float)(0.1 * nu));
             tm.sync();
         }
@@ -1149,12 +1149,12 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
             double rr[1];
             if (polish) {
                 if (comp > 0) {
-                    phase_velgrad(tm, M, I, 1 << (comp - 1));
+                    phase_velgrad<T, true>(tm, M, I, 1 << (comp - 1));
                     tm.sync();
                 }
-                phase_mom_faces(tm, M, I, comp);
+                phase_mom_faces<T, true>(tm, M, I, comp);
                 tm.sync();
-                phase_mom_cells(tm, M, I, comp);
+                phase_mom_cells<T, true>(tm, M, I, comp);
                 tm.sync();
                 rr[0] = px_defect(tm, M, I, u, false);
             } else {
@@ -1262,9 +1262,9 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
                     // solver (as in the reference): the polishing stage solves
                     // omega with the FP64 BiCGSTAB from the old omega, exactly as
                     // the FP64 engine does.
-                    phase_turb_faces(tm, M, I, which);
+                    phase_turb_faces<T, true>(tm, M, I, which);
                     tm.sync();
-                    phase_turb_cells(tm, M, I, which);
+                    phase_turb_cells<T, true>(tm, M, I, which);
                     for (int c = tm.rank(); c < nC; c += tm.size()) old[c] = phi[c];
                     tm.sync();
                     const SolveResult rw = team_bicgstab(tm, M, I, phi, S.innerIter, S.innerTol);
@@ -1275,9 +1275,9 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
                 } else {
                     double rr[1];
                     if (polish) {
-                        phase_turb_faces(tm, M, I, which);
+                        phase_turb_faces<T, true>(tm, M, I, which);
                         tm.sync();
-                        phase_turb_cells(tm, M, I, which);
+                        phase_turb_cells<T, true>(tm, M, I, which);
                         tm.sync();
                         rr[0] = px_defect(tm, M, I, phi, false);
                     } else {

@@ -66,11 +66,44 @@ __device__ __forceinline__ double sst_Pw(const Coef &c, double nuT, double S, do
     return smin(S2, lim);
 }
 
+// The same closure with FP64 reciprocals formed once per cell (the mixed
+// engine's FP64 polishing stage: FP64-accurate, not reference-rounded; GB300
+// spends tens of FP64 instructions on every division).
+struct SstCell { double F1, F2, nuT, Pk, CDkw; };
+__device__ __forceinline__ SstCell sst_cell_fast(const Coef &c, double kc, double wc, double y, double nu, double S,
+                                                 double gradDot) {
+    SstCell r;
+    const double kp = smax(kc, 0.0);
+    const double sqrtK = sqrt(kp);
+    const double rw = 1.0 / smax(wc, 1e-20);
+    const double ySafe = smax(y, 1e-20);
+    const double ry = 1.0 / ySafe;
+    const double ry2 = ry * ry;
+    r.CDkw = 2.0 * c.sw2 * rw * gradDot;
+    const double CDpos = smax(r.CDkw, 1e-20);
+    const double t1 = sqrtK * rw * ry / c.bstar;
+    const double t2 = 500.0 * nu * ry2 * rw;
+    if (c.variant == 2) {
+        r.F1 = 1.0;
+    } else {
+        const double t3 = 4.0 * c.sw2 * kp * ry2 / CDpos;
+        const double arg1 = smin(smax(t1, t2), t3);
+        const double a2 = arg1 * arg1;
+        r.F1 = tanh(a2 * a2);
+    }
+    const double arg2 = smax(2.0 * t1, t2);
+    r.F2 = tanh(arg2 * arg2);
+    if (c.variant == 1) r.nuT = kp * rw;
+    else r.nuT = c.a1 * kp / smax(smax(c.a1 * wc, S * r.F2), 1e-20);
+    r.Pk = smin(r.nuT * S * S, 10.0 * c.bstar * kp * smax(wc, 1e-20));
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Green-Gauss gradients (core/include/Field.hpp:122-152): per cell, internal
 // faces in ascending face order, then boundary faces, then / V.
 // ---------------------------------------------------------------------------
-template <class T, int NF>
+template <class T, int NF, bool Fast = false>
 __device__ __forceinline__ void gg_cell(const DevMesh &M, int c, const double *const *phi,
                                         const double *const *phib, double *gx, double *gy, double *gz) {
     double ax[NF], ay[NF], az[NF], pc[NF];
@@ -114,36 +147,42 @@ __device__ __forceinline__ void gg_cell(const DevMesh &M, int c, const double *c
     }
     const double V = M.vol[c];
     if (V > 1e-30) {
+        if (Fast) {
+            const double rv = 1.0 / V;
 #pragma unroll
-        for (int q = 0; q < NF; ++q) { ax[q] = ax[q] / V; ay[q] = ay[q] / V; az[q] = az[q] / V; }
+            for (int q = 0; q < NF; ++q) { ax[q] *= rv; ay[q] *= rv; az[q] *= rv; }
+        } else {
+#pragma unroll
+            for (int q = 0; q < NF; ++q) { ax[q] = ax[q] / V; ay[q] = ay[q] / V; az[q] = az[q] / V; }
+        }
     }
 #pragma unroll
     for (int q = 0; q < NF; ++q) { gx[q] = ax[q]; gy[q] = ay[q]; gz[q] = az[q]; }
 }
 
 // gradient of one scalar into (gx, gy, gz)
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_grad1(T &tm, const DevMesh &M, const double *phi, const double *phib,
                             double *ox, double *oy, double *oz) {
     const double *P[1] = {phi};
     const double *PB[1] = {phib};
     for (int c = tm.rank(); c < M.nC; c += tm.size()) {
         double gx[1], gy[1], gz[1];
-        gg_cell<T, 1>(M, c, P, PB, gx, gy, gz);
+        gg_cell<T, 1, Fast>(M, c, P, PB, gx, gy, gz);
         ox[c] = gx[0]; oy[c] = gy[0]; oz[c] = gz[0];
     }
 }
 
 // velocity gradients (Field.hpp:232-246): g[3*i+j] = dU_i/dx_j; `which` selects
 // components (bit i) so a partially updated U only recomputes what changed
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_velgrad(T &tm, const DevMesh &M, DevInst &I, int which) {
     const double *U[3] = {I.ux, I.uy, I.uz};
     const double *UB[3] = {I.ubx, I.uby, I.ubz};
     for (int c = tm.rank(); c < M.nC; c += tm.size()) {
         if (which == 7) {
             double gx[3], gy[3], gz[3];
-            gg_cell<T, 3>(M, c, U, UB, gx, gy, gz);
+            gg_cell<T, 3, Fast>(M, c, U, UB, gx, gy, gz);
 #pragma unroll
             for (int i = 0; i < 3; ++i) { I.g[3 * i][c] = gx[i]; I.g[3 * i + 1][c] = gy[i]; I.g[3 * i + 2][c] = gz[i]; }
         } else {
@@ -152,7 +191,7 @@ __device__ __noinline__ void phase_velgrad(T &tm, const DevMesh &M, DevInst &I, 
                 const double *P[1] = {U[i]};
                 const double *PB[1] = {UB[i]};
                 double gx[1], gy[1], gz[1];
-                gg_cell<T, 1>(M, c, P, PB, gx, gy, gz);
+                gg_cell<T, 1, Fast>(M, c, P, PB, gx, gy, gz);
                 I.g[3 * i][c] = gx[0]; I.g[3 * i + 1][c] = gy[0]; I.g[3 * i + 2][c] = gz[0];
             }
         }
@@ -161,7 +200,7 @@ __device__ __noinline__ void phase_velgrad(T &tm, const DevMesh &M, DevInst &I, 
 
 // SSTModel::computeFields + frozen |S| + startup floor (SIMPLESolver.cpp:736-768).
 // Requires velocity gradients in I.g.  nutMin < 0 skips the floor.
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_sst(T &tm, const DevMesh &M, DevInst &I, double nutMin) {
     const Coef cf = load_coef(I);
     const double nu = I.nu;
@@ -174,10 +213,20 @@ __device__ __noinline__ void phase_sst(T &tm, const DevMesh &M, DevInst &I, doub
         double S23 = 0.5 * (LD(I.g[5] + c) + LD(I.g[7] + c));
         double Sc = sqrt(2.0 * (S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23)));
         double gx[2], gy[2], gz[2];
-        gg_cell<T, 2>(M, c, P, PB, gx, gy, gz);
+        gg_cell<T, 2, Fast>(M, c, P, PB, gx, gy, gz);
         double kc = smax(LD(I.k + c), 0.0);
         double wc = smax(LD(I.om + c), 1e-20);
         double y = smax(M.wd[c], 1e-20);
+        if (Fast) {
+            const SstCell r = sst_cell_fast(cf, kc, wc, y, nu, Sc, gx[0] * gx[1] + gy[0] * gy[1] + gz[0] * gz[1]);
+            I.smag[c] = Sc;
+            I.cdkw[c] = r.CDkw;
+            I.f1[c] = r.F1;
+            I.f2[c] = r.F2;
+            I.pk[c] = r.Pk;
+            I.nut[c] = (nutMin < 0.0) ? r.nuT : smax(r.nuT, nutMin);
+            continue;
+        }
         double omSafe = smax(wc, 1e-20);
         double CDkw = 2.0 * cf.sw2 / omSafe * (gx[0] * gx[1] + gy[0] * gy[1] + gz[0] * gz[1]);
         double CDpos = smax(CDkw, 1e-20);
@@ -199,7 +248,7 @@ __device__ __noinline__ void phase_sst(T &tm, const DevMesh &M, DevInst &I, doub
 // ---------------------------------------------------------------------------
 // Face pass of the momentum system: upper/lower coefficients and the
 // transpose-stress flux of component `comp` (StressOperators.hpp:331-340).
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_mom_faces(T &tm, const DevMesh &M, DevInst &I, int comp) {
     const double nu = I.nu;
     const double *gc0 = I.g[comp], *gc1 = I.g[3 + comp], *gc2 = I.g[6 + comp];
@@ -210,7 +259,7 @@ __device__ __noinline__ void phase_mom_faces(T &tm, const DevMesh &M, DevInst &I
         double nuEff_o = nu + nuo;
         double nuEff_n = nu + nun;
         double nuEff_f = w * nuEff_o + (1.0 - w) * nuEff_n;
-        double Df = nuEff_f * Sf / delta;
+        double Df = Fast ? nuEff_f * M.aOverD[f] : nuEff_f * Sf / delta;
         double Ufx = LD(I.ux + o) * w + LD(I.ux + n) * (1.0 - w);
         double Ufy = LD(I.uy + o) * w + LD(I.uy + n) * (1.0 - w);
         double Ufz = LD(I.uz + o) * w + LD(I.uz + n) * (1.0 - w);
@@ -229,10 +278,11 @@ __device__ __noinline__ void phase_mom_faces(T &tm, const DevMesh &M, DevInst &I
 }
 
 // Cell pass of the momentum system (diag, source, relaxation).
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_mom_cells(T &tm, const DevMesh &M, DevInst &I, int comp) {
     const double nu = I.nu;
     const double alphaU = I.S.alphaU;
+    const double relaxDiag = 1.0 / alphaU, relaxSrc = (1.0 - alphaU) / alphaU;
     const double fb = I.S.bodyForce[comp];
     const double *Uc = comp == 0 ? I.ux : (comp == 1 ? I.uy : I.uz);
     const double *Ubc = comp == 0 ? I.ubx : (comp == 1 ? I.uby : I.ubz);
@@ -257,7 +307,7 @@ __device__ __noinline__ void phase_mom_cells(T &tm, const DevMesh &M, DevInst &I
             const int b = M.cbFace[e];
             const double Sf = M.barea[b], delta = M.bdeltaC[b];
             double nuEff = (M.bwall[b] && !wallFn) ? nu : nu + nutc;
-            double Db = nuEff * Sf / delta;
+            double Db = Fast ? nuEff * M.baOverD[b] : nuEff * Sf / delta;
             double Ub = LD(Ubc + b);
             double mFlux = (LD(I.ubx + b) * M.bnx[b] + LD(I.uby + b) * M.bny[b] + LD(I.ubz + b) * M.bnz[b]) * Sf;
             if (mFlux >= 0) {
@@ -281,8 +331,13 @@ __device__ __noinline__ void phase_mom_cells(T &tm, const DevMesh &M, DevInst &I
         if (fb != 0.0) src = src + fb * vol;
         src = src + ts;
         const double phi_old = LD(Uc + c);
-        src = src + (1.0 - alphaU) / alphaU * diag * phi_old;
-        diag = diag / alphaU;
+        if (Fast) {
+            src = src + relaxSrc * diag * phi_old;
+            diag = diag * relaxDiag;
+        } else {
+            src = src + (1.0 - alphaU) / alphaU * diag * phi_old;
+            diag = diag / alphaU;
+        }
         I.diag[c] = diag;
         I.src[c] = src;
         if (comp == 0) I.aPx[c] = diag;
@@ -348,7 +403,7 @@ __device__ __noinline__ void phase_p_cells(T &tm, const DevMesh &M, DevInst &I) 
 }
 
 // k (which = 0) or omega (which = 1) face pass
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_turb_faces(T &tm, const DevMesh &M, DevInst &I, int which) {
     const Coef cf = load_coef(I);
     const double nu = I.nu;
@@ -361,7 +416,7 @@ __device__ __noinline__ void phase_turb_faces(T &tm, const DevMesh &M, DevInst &
         double nuEff_o = nu + sg * LD(I.nut + o);
         double nuEff_n = nu + sg * LD(I.nut + n);
         double nuEff_f = w * nuEff_o + (1.0 - w) * nuEff_n;
-        double Df = nuEff_f * Sf / delta;
+        double Df = Fast ? nuEff_f * M.aOverD[f] : nuEff_f * Sf / delta;
         double Ufx = LD(I.ux + o) * w + LD(I.ux + n) * (1.0 - w);
         double Ufy = LD(I.uy + o) * w + LD(I.uy + n) * (1.0 - w);
         double Ufz = LD(I.uz + o) * w + LD(I.uz + n) * (1.0 - w);
@@ -373,7 +428,7 @@ __device__ __noinline__ void phase_turb_faces(T &tm, const DevMesh &M, DevInst &
     }
 }
 
-template <class T>
+template <class T, bool Fast = false>
 __device__ __noinline__ void phase_turb_cells(T &tm, const DevMesh &M, DevInst &I, int which) {
     const Coef cf = load_coef(I);
     const double nu = I.nu;
@@ -381,6 +436,7 @@ __device__ __noinline__ void phase_turb_cells(T &tm, const DevMesh &M, DevInst &
     const double *phib = which == 0 ? I.kb : I.omb;
     const double *phi = which == 0 ? I.k : I.om;
     const double alpha = which == 0 ? I.S.alphaK : I.S.alphaW;
+    const double relaxDiag = 1.0 / alpha, relaxSrc = (1.0 - alpha) / alpha;
     for (int c = tm.rank(); c < M.nC; c += tm.size()) {
         double diag = 0.0, src = 0.0;
         for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
@@ -394,7 +450,7 @@ __device__ __noinline__ void phase_turb_cells(T &tm, const DevMesh &M, DevInst &
             const double Sf = M.barea[b], delta = M.bdeltaC[b];
             double sg = blend(s1, s2, F1c);
             double nuEff = nu + sg * nutc;
-            double Db = nuEff * Sf / delta;
+            double Db = Fast ? nuEff * M.baOverD[b] : nuEff * Sf / delta;
             double vb = LD(phib + b);
             double mFlux = (LD(I.ubx + b) * M.bnx[b] + LD(I.uby + b) * M.bny[b] + LD(I.ubz + b) * M.bnz[b]) * Sf;
             if (mFlux >= 0) {
@@ -420,8 +476,13 @@ __device__ __noinline__ void phase_turb_cells(T &tm, const DevMesh &M, DevInst &
             diag = diag + betaB * omC * vol;
             src = src + (1.0 - F1c) * LD(I.cdkw + c) * vol;
         }
-        src = src + (1.0 - alpha) / alpha * diag * LD(phi + c);
-        diag = diag / alpha;
+        if (Fast) {
+            src = src + relaxSrc * diag * LD(phi + c);
+            diag = diag * relaxDiag;
+        } else {
+            src = src + (1.0 - alpha) / alpha * diag * LD(phi + c);
+            diag = diag / alpha;
+        }
         I.diag[c] = diag;
         I.src[c] = src;
     }
