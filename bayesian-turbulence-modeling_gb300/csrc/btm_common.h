@@ -106,7 +106,8 @@ struct DevWork32 {
     float *tflux;          // [nIF] transpose-stress face flux
     float *dcoef;          // [nIF] diffusion coefficient D_f of the equation being assembled
     float *r, *rh, *pv, *v, *s, *t, *ph, *sh, *rd, *x;
-    float *amgVal, *amgX, *amgB, *amgR, *amgRd, *ainv, *gj;
+    float *amgVal, *amgX, *amgB, *amgR, *amgRd;
+    double *ainv, *gj;     // FP64 dense inverse of the coarsest level and its Gauss-Jordan buffers
     double *mflux;         // [nIF] FP64 face mass flux (convective defect, continuity defect)
     double *src64;         // [nC] FP64 pressure-correction right-hand side (refinement)
 };
@@ -168,9 +169,12 @@ int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream);
 int engine_launch_grid(DevInst *dInst, int blocks, void *stream);
 int engine_grid_blocks(int *blocks_out);
 int engine_launch_debug(DevInst *dInst, void *stream);
+int engine_wall_distance(const double *dCentres, int nC, const double *dWall, int nW, double *dOut, void *stream);
 
 // mixed-precision engine entry points (btm_mixed.cu)
 size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN);
 int mixed_launch_block(DevInst *dInsts, int n, int threads, size_t smemBytes, void *stream);
+int mixed_grid_blocks(int *blocks_out);
+int mixed_launch_grid(DevInst *dInst, int blocks, void *stream);
 
 }  // namespace btm

@@ -781,6 +781,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_debug(DevInst *inst) {
 }
 
 // ---------------------------------------------------------------------------
+// Mesh::computeWallDistance (core/src/Mesh.cpp:345-373): minimum over the wall
+// face centres of |c - w|.  Each thread owns one cell; the wall centres stream
+// through shared memory in tiles.  The squared distance is formed exactly as
+// (dx*dx + dy*dy) + dz*dz without contraction and the square root is taken
+// once of the minimum: sqrt is correctly rounded and monotone, so the result
+// is bit-identical to the reference's minimum of square roots.
+// ---------------------------------------------------------------------------
+constexpr int kWallTile = 1024;
+__global__ void __launch_bounds__(256) k_wall_distance(const double *cc, int nC, const double *wp, int nW,
+                                                        double *out) {
+    __shared__ double sx[kWallTile], sy[kWallTile], sz[kWallTile];
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double x = 0.0, y = 0.0, z = 0.0;
+    if (c < nC) { x = cc[3 * (size_t)c]; y = cc[3 * (size_t)c + 1]; z = cc[3 * (size_t)c + 2]; }
+    double best = INFINITY;
+    for (int t0 = 0; t0 < nW; t0 += kWallTile) {
+        const int n = min(kWallTile, nW - t0);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            sx[j] = wp[3 * (size_t)(t0 + j)];
+            sy[j] = wp[3 * (size_t)(t0 + j) + 1];
+            sz[j] = wp[3 * (size_t)(t0 + j) + 2];
+        }
+        __syncthreads();
+        for (int j = 0; j < n; ++j) {
+            const double dx = __dsub_rn(x, sx[j]), dy = __dsub_rn(y, sy[j]), dz = __dsub_rn(z, sz[j]);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            best = d2 < best ? d2 : best;
+        }
+        __syncthreads();
+    }
+    if (c < nC) out[c] = sqrt(best);
+}
+
+int engine_wall_distance(const double *dCentres, int nC, const double *dWall, int nW, double *dOut, void *stream) {
+    if (nC <= 0) return 0;
+    k_wall_distance<<<(nC + 255) / 256, 256, 0, (cudaStream_t)stream>>>(dCentres, nC, dWall, nW, dOut);
+    return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
 int engine_block_threads() { return kThreads; }

@@ -682,7 +682,7 @@ void ensure_mixed(btm_case *C, Slab &S) {
     floats += 32 * cell;                      // cell arrays
     floats += up((size_t)nC + 2 * (size_t)nIF) + 2 * face + bnd;
     floats += up(std::max<int64_t>(C->amgValTotal, 1)) + 3 * up(std::max<int64_t>(C->amgVecTotal, 1)) +
-              up((size_t)nC + C->amgVecTotal) + up((size_t)nc * nc) + up((size_t)4 * nc * nc);
+              up((size_t)nC + C->amgVecTotal) + up((size_t)2 * nc * nc) + up((size_t)8 * nc * nc);
     floats += 2 * face + 2 * cell;            // FP64 mass flux [nIF] and right-hand side [nC]
     const size_t bytes = floats * 4 + 512;
     char *base = nullptr;
@@ -709,8 +709,8 @@ void ensure_mixed(btm_case *C, Slab &S) {
     F.amgB = take(std::max<int64_t>(C->amgVecTotal, 1));
     F.amgR = take(std::max<int64_t>(C->amgVecTotal, 1));
     F.amgRd = take((size_t)nC + C->amgVecTotal);
-    F.ainv = take((size_t)nc * nc);
-    F.gj = take((size_t)4 * nc * nc);
+    F.ainv = (double *)take((size_t)2 * nc * nc);
+    F.gj = (double *)take((size_t)8 * nc * nc);
     F.mflux = (double *)take(2 * (size_t)std::max(nIF, 1));
     F.src64 = (double *)take(2 * (size_t)nC);
     if ((size_t)((char *)d - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "fp32 slab overflow");
@@ -937,14 +937,10 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             }
             ck(cudaMemsetAsync(I.barrier, 0, 512, st), "memset control");
             const bool mixed = J.C->settings.precision == BTM_PREC_MIXED;
-            if (mixed) {
-                if (J.C->nC > block_max_cells())
-                    throw BtmError(BTM_ERR_ARG, "mixed precision runs meshes of up to " +
-                                                    std::to_string(block_max_cells()) +
-                                                    " cells (one CTA per instance); use fp64 for larger meshes");
-                ensure_mixed(J.C, *J.S);
+            if (mixed) ensure_mixed(J.C, *J.S);
+            if (mixed && J.C->nC <= block_max_cells()) {
                 mixIdx.push_back(i);
-            } else if (J.C->nC <= block_max_cells()) {
+            } else if (!mixed && J.C->nC <= block_max_cells()) {
                 blockIdx.push_back(i);
             } else {
                 gridIdx.push_back(i);
@@ -991,7 +987,15 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             ck(cudaMalloc((void **)&dI, sizeof(btm::DevInst)), "cudaMalloc(inst)");
             ck(cudaMemcpyAsync(dI, &jobs[i].S->inst, sizeof(btm::DevInst), cudaMemcpyHostToDevice, st), "inst");
             gridPtrs.push_back(dI);
-            int e = btm::engine_launch_grid(dI, jobs[i].C->maxGridBlocks, st);
+            int e;
+            if (jobs[i].C->settings.precision == BTM_PREC_MIXED) {
+                int mb = 0;
+                e = btm::mixed_grid_blocks(&mb);
+                // the grid reduction buffers of the slab hold maxGridBlocks CTAs
+                if (!e) e = btm::mixed_launch_grid(dI, std::min(mb, jobs[i].C->maxGridBlocks), st);
+            } else {
+                e = btm::engine_launch_grid(dI, jobs[i].C->maxGridBlocks, st);
+            }
             if (e) throw BtmError(BTM_ERR_CUDA, std::string("grid launch: ") + cudaGetErrorString((cudaError_t)e));
         }
         ck(cudaEventRecord(ev1, st), "event");
@@ -1054,6 +1058,33 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
     } catch (const std::exception &e) {
         return fail(BTM_ERR_INTERNAL, e.what());
     }
+    return BTM_OK;
+}
+
+int btm_wall_distance(int32_t n_cells, const double *cell_centre, int32_t n_wall, const double *wall_centre,
+                      double *out) {
+    if (n_cells < 0 || n_wall < 0 || (n_cells > 0 && (!cell_centre || !out)) || (n_wall > 0 && !wall_centre))
+        return fail(BTM_ERR_ARG, "bad wall-distance arguments");
+    if (n_cells == 0) return BTM_OK;
+    if (n_wall == 0) {
+        for (int c = 0; c < n_cells; ++c) out[c] = 1e10;
+        return BTM_OK;
+    }
+    if (int e = ensure_device()) return e;
+    double *d = nullptr;
+    const size_t nc = (size_t)n_cells, nw = (size_t)n_wall;
+    try {
+        ck(cudaMalloc((void **)&d, 8 * (3 * nc + 3 * nw + nc)), "cudaMalloc(wall distance)");
+        ck(cudaMemcpy(d, cell_centre, 8 * 3 * nc, cudaMemcpyHostToDevice), "upload");
+        ck(cudaMemcpy(d + 3 * nc, wall_centre, 8 * 3 * nw, cudaMemcpyHostToDevice), "upload");
+        int e = btm::engine_wall_distance(d, n_cells, d + 3 * nc, n_wall, d + 3 * nc + 3 * nw, nullptr);
+        if (e) throw BtmError(BTM_ERR_CUDA, std::string("wall distance: ") + cudaGetErrorString((cudaError_t)e));
+        ck(cudaMemcpy(out, d + 3 * nc + 3 * nw, 8 * nc, cudaMemcpyDeviceToHost), "download");
+    } catch (const BtmError &e) {
+        if (d) cudaFree(d);
+        return fail(e.code, e.what());
+    }
+    cudaFree(d);
     return BTM_OK;
 }
 

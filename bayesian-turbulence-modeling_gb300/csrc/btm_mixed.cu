@@ -243,10 +243,10 @@ __device__ __forceinline__ void cd_face(const DevMesh &M, DevInst &I, int f, flo
     n = M.nbr[f];
     w = G.w[f];
     wn = 1.0f - w;
-    const float nuo = F.nut[o], nun = F.nut[n];
+    const float nuo = LD(F.nut + o), nun = LD(F.nut + n);
     float Df;
     if (sg1 >= 0.0f) {
-        const float sg = blendf(sg1, sg2, w * F.f1[o] + wn * F.f1[n]);
+        const float sg = blendf(sg1, sg2, w * LD(F.f1 + o) + wn * LD(F.f1 + n));
         Df = (w * (nu + sg * nuo) + wn * (nu + sg * nun)) * G.area[f] * G.rdelta[f];
     } else {
         Df = (w * (nu + nuo) + wn * (nu + nun)) * G.area[f] * G.rdelta[f];
@@ -277,8 +277,9 @@ __device__ __noinline__ void mx_mom_faces(T &tm, const DevMesh &M, DevInst &I, i
         float w, wn;
         int o, n;
         cd_face<T>(M, I, f, nu, -1.0f, 0.0f, true, z, w, wn, o, n);
-        const float cfac = w * F.nut[o] + wn * F.nut[n];
-        const float gx = gc0[o] * w + gc0[n] * wn, gy = gc1[o] * w + gc1[n] * wn, gz = gc2[o] * w + gc2[n] * wn;
+        const float cfac = w * LD(F.nut + o) + wn * LD(F.nut + n);
+        const float gx = LD(gc0 + o) * w + LD(gc0 + n) * wn, gy = LD(gc1 + o) * w + LD(gc1 + n) * wn,
+                    gz = LD(gc2 + o) * w + LD(gc2 + n) * wn;
         F.tflux[f] = cfac * (gx * G.nx[f] + gy * G.ny[f] + gz * G.nz[f]) * G.area[f];
     }
 }
@@ -298,16 +299,16 @@ __device__ __forceinline__ double cd_cell_flux(const DevMesh &M, const DevInst &
         int other;
         double mo;
         if (oth >= 0) {
-            diag -= F.lower[f];
+            diag -= LD(F.lower + f);
             other = oth;
             mo = LD(F.mflux + f);
         } else {
-            diag -= F.upper[f];
+            diag -= LD(F.upper + f);
             other = -(oth + 1);
             mo = -LD(F.mflux + f);
         }
         const double phiN = LD(phi + other);
-        r = fma((double)F.dcoef[f], phiP - phiN, r);
+        r = fma((double)LD(F.dcoef + f), phiP - phiN, r);
         r = fma(mo, mo >= 0.0 ? phiP : phiN, r);
     }
     return r;
@@ -335,7 +336,7 @@ __device__ __noinline__ double mx_mom_cells(T &tm, const DevMesh &M, DevInst &I,
         double flux = cd_cell_flux<T>(M, I, c, Uc, uP, diag);
         for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
             const int f = M.cfFace[e];
-            ts += M.cfOther[e] >= 0 ? F.tflux[f] : -F.tflux[f];
+            ts += M.cfOther[e] >= 0 ? LD(F.tflux + f) : -LD(F.tflux + f);
         }
         const float nutc = F.nut[c];
         for (int e = M.cbOff[c]; e < M.cbOff[c + 1]; ++e) {
@@ -378,7 +379,7 @@ __device__ __noinline__ void mx_p_faces(T &tm, const DevMesh &M, DevInst &I) {
     for (int f = tm.rank(); f < M.nIF; f += tm.size()) {
         const int o = M.own[f], n = M.nbr[f];
         const float Sf = G.area[f], w = G.w[f], wn = 1.0f - w;
-        const float aPo = F.aPx[o], aPn = F.aPx[n];
+        const float aPo = LD(F.aPx + o), aPn = LD(F.aPx + n);
         const float dP_o = (fabsf(aPo) > 1e-30f) ? G.vol[o] / aPo : 0.0f;
         const float dP_n = (fabsf(aPn) > 1e-30f) ? G.vol[n] / aPn : 0.0f;
         const float dP_f = w * dP_o + wn * dP_n;
@@ -387,9 +388,9 @@ __device__ __noinline__ void mx_p_faces(T &tm, const DevMesh &M, DevInst &I) {
         F.lower[f] = -coeff;
         double mf = mflux64<T>(M, I, f, o, n, z);
         if (rc) {
-            const float gbx = F.gp[0][o] * w + F.gp[0][n] * wn;
-            const float gby = F.gp[1][o] * w + F.gp[1][n] * wn;
-            const float gbz = F.gp[2][o] * w + F.gp[2][n] * wn;
+            const float gbx = LD(F.gp[0] + o) * w + LD(F.gp[0] + n) * wn;
+            const float gby = LD(F.gp[1] + o) * w + LD(F.gp[1] + n) * wn;
+            const float gbz = LD(F.gp[2] + o) * w + LD(F.gp[2] + n) * wn;
             const float dp = (float)(LD(I.p + n) - LD(I.p + o));
             const float d = -dP_f * Sf * (dp * G.rdelta[f] - (gbx * G.ex[f] + gby * G.ey[f] + gbz * G.ez[f]));
             mf += (double)d;
@@ -410,7 +411,7 @@ __device__ __noinline__ double mx_p_cells(T &tm, const DevMesh &M, DevInst &I) {
         double src = 0.0;
         for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
             const int f = M.cfFace[e];
-            diag -= F.upper[f];
+            diag -= LD(F.upper + f);
             if (M.cfOther[e] >= 0) src -= LD(F.mflux + f);
             else src += LD(F.mflux + f);
         }
@@ -647,17 +648,22 @@ __device__ void mx_amg_level_rd(T &tm, const DevMesh &M, DevWork32 &F, int l) {
     }
 }
 
-// dense inverse of the coarsest level (Gauss-Jordan, ping-pong buffers)
+// Dense inverse of the coarsest level (Gauss-Jordan, ping-pong buffers), in
+// FP64: the coarsest Galerkin matrix of a pinned pure-Neumann pressure system
+// is nearly singular (its condition grows with the mesh), and an FP32 inverse
+// of it wrecked the preconditioner on a 2M-cell duct (39 PCG iterations per
+// solve instead of about one).  At most 32 rows, refreshed every
+// kAmgRefresh outer iterations.
 template <class T>
 __device__ __noinline__ void mx_amg_coarse_inverse(T &tm, const DevMesh &M, DevWork32 &F) {
     const int l = M.nLevels - 1;
     const AmgLevelDev &L = M.lev[l];
     const int n = L.n, w2 = 2 * n;
-    float *A = F.gj, *B = F.gj + (size_t)n * w2;
+    double *A = F.gj, *B = F.gj + (size_t)n * w2;
     const float *val = lev_valsf(F, M, l);
     for (int i = tm.rank(); i < n; i += tm.size()) {
-        float *row = A + (size_t)i * w2;
-        for (int j = 0; j < w2; ++j) row[j] = 0.0f;
+        double *row = A + (size_t)i * w2;
+        for (int j = 0; j < w2; ++j) row[j] = 0.0;
         if (l == 0) {
             row[i] = LD(F.diag + i);
             for (int e = M.cfOff[i]; e < M.cfOff[i + 1]; ++e) {
@@ -668,25 +674,25 @@ __device__ __noinline__ void mx_amg_coarse_inverse(T &tm, const DevMesh &M, DevW
         } else {
             for (int q = L.rowPtr[i]; q < L.rowPtr[i + 1]; ++q) row[L.colIdx[q]] = LD(val + q);
         }
-        row[n + i] = 1.0f;
+        row[n + i] = 1.0;
     }
     tm.sync();
     for (int k = 0; k < n; ++k) {
-        const float piv = LD(A + (size_t)k * w2 + k);
-        const bool skip = !(fabsf(piv) > 1e-37f);
-        const float rp = skip ? 0.0f : 1.0f / piv;
+        const double piv = LD(A + (size_t)k * w2 + k);
+        const bool skip = !(fabs(piv) > 1e-300);
+        const double rp = skip ? 0.0 : 1.0 / piv;
         for (int idx = tm.rank(); idx < n * w2; idx += tm.size()) {
             const int i = idx / w2, j = idx - i * w2;
-            const float akj = LD(A + (size_t)k * w2 + j) * rp;
-            float v = LD(A + idx);
+            const double akj = LD(A + (size_t)k * w2 + j) * rp;
+            double v = LD(A + idx);
             if (!skip) {
                 if (i == k) v = akj;
-                else v = fmaf(-LD(A + (size_t)i * w2 + k), akj, v);
+                else v = fma(-LD(A + (size_t)i * w2 + k), akj, v);
             }
             B[idx] = v;
         }
         tm.sync();
-        float *tmp = A; A = B; B = tmp;
+        double *tmp = A; A = B; B = tmp;
     }
     for (int idx = tm.rank(); idx < n * n; idx += tm.size()) {
         const int i = idx / n, j = idx - i * n;
@@ -789,9 +795,9 @@ __device__ void mx_amg_coarse_solve(T &tm, const DevMesh &M, DevWork32 &F) {
         const float *b = lev_bf(F, M, l);
         float *x = lev_xf(F, M, l);
         for (int i = tm.rank(); i < n; i += tm.size()) {
-            float s = 0.0f;
-            for (int j = 0; j < n; ++j) s = fmaf(LD(F.ainv + (size_t)i * n + j), LD(b + j), s);
-            x[i] = s;
+            double s = 0.0;
+            for (int j = 0; j < n; ++j) s = fma(LD(F.ainv + (size_t)i * n + j), (double)LD(b + j), s);
+            x[i] = (float)s;
         }
         tm.sync();
     } else {
@@ -814,14 +820,20 @@ __device__ void mx_amg_values_from(T &tm, const DevMesh &M, DevWork32 &F, int l0
 
 // symmetric V-cycle on levels [l0, nLevels): 2 pre-sweeps (colours
 // ascending), 2 post-sweeps (colours descending)
-// two smoothing sweeps of level l: multicolour Gauss-Seidel on level 0
-// (colours ascending before the coarse correction, descending after), a pair
-// of damped-Jacobi sweeps (x -> r -> x) on coarser levels
+// two smoothing sweeps of level l: multicolour Gauss-Seidel (colours
+// ascending before the coarse correction, descending after); on the coarse
+// levels of a one-CTA instance a pair of damped-Jacobi sweeps (x -> r -> x)
+// instead, which needs no colour barriers and cost ~20 % more PCG iterations
+// on 2-D meshes (on a 3-D 2M-cell duct it cost 30x: grid-mode instances keep
+// Gauss-Seidel)
+template <class T> struct CoarseJacobi { static constexpr bool value = false; };
+template <> struct CoarseJacobi<BlockTeam> { static constexpr bool value = true; };
+
 template <class T>
 __device__ void mx_amg_smooth2(T &tm, const DevMesh &M, DevWork32 &F, int l, bool post) {
-    if (l == 0) {
-        mx_amg_gs_sweep(tm, M, F, 0, post);
-        mx_amg_gs_sweep(tm, M, F, 0, post);
+    if (l == 0 || !CoarseJacobi<T>::value) {
+        mx_amg_gs_sweep(tm, M, F, l, post);
+        mx_amg_gs_sweep(tm, M, F, l, post);
     } else {
         float *x = lev_xf(F, M, l), *tmp = lev_rf(F, M, l);
         mx_amg_jacobi(tm, M, F, l, x, tmp);
@@ -862,6 +874,53 @@ __device__ void mx_amg_setup(T &tm, const DevMesh &M, DevWork32 &F, bool coarse 
 template <class T>
 __device__ void mx_amg_vcycle(T &tm, const DevMesh &M, DevWork32 &F) {
     mx_amg_vcycle_from(tm, M, F, 0);
+}
+
+// Grid-team setup and V-cycle (meshes above the one-CTA size): levels of at
+// least kGridLevelRows rows run on the whole cooperative grid, the coarser
+// ones on CTA 0 alone (its loads bypass L1 like the grid's).
+constexpr int kGridLevelRows = 16384;
+
+__device__ __forceinline__ int mx_grid_split(const DevMesh &M) {
+    int l = 0;
+    while (l < M.nLevels - 1 && M.lev[l].n >= kGridLevelRows) ++l;
+    return l;
+}
+
+__device__ void mx_amg_setup(GridTeam &tm, const DevMesh &M, DevWork32 &F, bool coarse = true) {
+    const int ls = mx_grid_split(M);
+    mx_amg_level_rd(tm, M, F, 0);
+    tm.sync();
+    if (!coarse) return;
+    for (int l = 1; l <= ls && l < M.nLevels; ++l) {
+        mx_amg_galerkin(tm, M, F, l);
+        tm.sync();
+        mx_amg_level_rd(tm, M, F, l);
+        tm.sync();
+    }
+    if (blockIdx.x == 0) {
+        BlockTeamCG bt{{tm.red, tm.buf}};
+        mx_amg_values_from(bt, M, F, ls + 1);
+        if (M.coarseDirect) mx_amg_coarse_inverse(bt, M, F);
+    }
+    tm.sync();
+}
+
+__device__ void mx_amg_vcycle(GridTeam &tm, const DevMesh &M, DevWork32 &F) {
+    const int ls = mx_grid_split(M);
+    for (int l = 0; l < ls; ++l) {
+        mx_amg_smooth2(tm, M, F, l, false);
+        mx_amg_restrict(tm, M, F, l);
+    }
+    if (blockIdx.x == 0) {
+        BlockTeamCG bt{{tm.red, tm.buf}};
+        mx_amg_vcycle_from(bt, M, F, ls);
+    }
+    tm.sync();
+    for (int l = ls - 1; l >= 0; --l) {
+        mx_amg_prolong(tm, M, F, l);
+        mx_amg_smooth2(tm, M, F, l, true);
+    }
 }
 
 // AMG-preconditioned CG (AMGSolver::solve, LinearSolver.hpp:602-653):
@@ -1227,7 +1286,7 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         }
         tm.sync();
         clk.lap(5);
-        for (int b = tm.rank(); b < nB; b += tm.size()) F.ppb[b] = M.bcPp[b] == 0 ? F.pp[M.bown[b]] : 0.0f;
+        for (int b = tm.rank(); b < nB; b += tm.size()) F.ppb[b] = M.bcPp[b] == 0 ? LD(F.pp + M.bown[b]) : 0.0f;
         tm.sync();
         // 4. corrections (correctVelocity / correctPressure, SIMPLESolver.cpp:456-475)
         {
@@ -1457,7 +1516,7 @@ __device__ __host__ inline int smem_items(int nC, int nIF, int64_t vec, int64_t 
     for (int i = 0; i < 3; ++i) sz[q++] = 4 * (size_t)(vec > 0 ? vec : 1);   // amgX amgB amgR
     sz[q++] = 4 * (size_t)(val > 0 ? val : 1);                      // amgVal
     for (int i = 0; i < 5; ++i) sz[q++] = 4 * (size_t)nC;           // rh ph sh rd src
-    sz[q++] = 4 * (size_t)nc * nc;                                  // coarse inverse
+    sz[q++] = 8 * (size_t)nc * nc;                                  // coarse inverse (FP64)
     sz[q++] = 4 * ((size_t)nC + 1);                                 // cfOff
     sz[q++] = 4 * (size_t)nGather;                                  // cfFace
     sz[q++] = 4 * (size_t)nGather;                                  // cfOther
@@ -1498,7 +1557,7 @@ __device__ void stage_smem(DevMesh &M, DevInst &I, unsigned char *dsm, size_t ca
             case 15: F.sh = f; break;
             case 16: F.rd = f; break;
             case 17: F.src = f; break;
-            case 18: F.ainv = f; break;
+            case 18: F.ainv = (double *)p; break;
             case 19: copies[nc_++] = {p, M.cfOff, (int)sz[q]}; M.cfOff = (const int32_t *)p; break;
             case 20: copies[nc_++] = {p, M.cfFace, (int)sz[q]}; M.cfFace = (const int32_t *)p; break;
             case 21: copies[nc_++] = {p, M.cfOther, (int)sz[q]}; M.cfOther = (const int32_t *)p; break;
@@ -1536,6 +1595,39 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_mixed_block(DevInst *insts, in
 }
 template __global__ void k_mixed_block<256>(DevInst *, int, int);
 template __global__ void k_mixed_block<512>(DevInst *, int, int);
+
+// One large instance over a cooperative grid (meshes above the one-CTA size).
+constexpr int kMixGridThreads = 512;
+__global__ void __launch_bounds__(kMixGridThreads, 1) k_mixed_grid(DevInst *inst) {
+    __shared__ double red[2 * 32 * kRedSlots];
+    __shared__ DevMesh sM;
+    __shared__ DevInst sI;
+    __shared__ int shAbort;
+    if (threadIdx.x == 0) {
+        sI = *inst;
+        sM = *sI.M;
+        shAbort = 0;
+    }
+    __syncthreads();
+    GridTeam tm{red, 0, sI.gpart, sI.barrier, sI.err, &shAbort};
+    mixed_solve(tm, sM, sI);
+}
+
+int mixed_grid_blocks(int *blocks_out) {
+    int dev = 0, sms = 0, per = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mixed_grid, kMixGridThreads, 0);
+    if (e != cudaSuccess) return (int)e;
+    *blocks_out = sms * (per < 1 ? 1 : per);
+    return 0;
+}
+
+int mixed_launch_grid(DevInst *dInst, int blocks, void *stream) {
+    void *args[] = {&dInst};
+    return (int)cudaLaunchCooperativeKernel((const void *)k_mixed_grid, dim3(blocks), dim3(kMixGridThreads), args, 0,
+                                            (cudaStream_t)stream);
+}
 
 // dynamic shared memory that would hold an instance's whole solver working set
 size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN) {

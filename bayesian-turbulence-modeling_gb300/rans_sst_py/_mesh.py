@@ -289,15 +289,29 @@ class Mesh:
         self._compute_face_geometry()
         self._compute_interpolation_weights()
 
-    def compute_wall_distance(self, chunk: int = 1 << 22) -> None:
+    def compute_wall_distance(self, chunk: int = 1 << 22, device: bool = False) -> None:
         """Mesh::computeWallDistance (core/src/Mesh.cpp:345-373): brute-force
-        minimum over the wall-patch face centres of |c - wp|, 1e10 without walls."""
+        minimum over the wall-patch face centres of |c - wp|, 1e10 without walls.
+        device=True runs the same O(n_cells * n_wall) search on the GPU
+        (btm_wall_distance, bit-identical)."""
         wall = [p[2] for p in self.patches if p[1] == "wall"]
         nC = self.n_cells()
         if not wall or sum(w.size for w in wall) == 0:
             self.wall_dist = np.full(nC, 1e10)
             return
         wp = self.face_center[np.concatenate(wall)]
+        if device:
+            import ctypes as C
+            from ._lib import check, dptr, lib
+            cc = np.ascontiguousarray(self.cell_center, np.float64)
+            wpc = np.ascontiguousarray(wp, np.float64)
+            out = np.empty(nC)
+            L = lib()
+            L.btm_wall_distance.argtypes = [C.c_int32, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]
+            check(L.btm_wall_distance(nC, dptr(cc), wpc.shape[0], dptr(wpc), dptr(out)))
+            self.wall_dist = out
+            return
         out = np.empty(nC)
         step = max(1, chunk // max(1, wp.shape[0]))
         for s in range(0, nC, step):

@@ -271,7 +271,14 @@ double btm_last_launch_ms(void);
 #define BTM_PHASE_SPMV          7   /* LinearSystem::matvec                    */
 #define BTM_PHASE_BICGSTAB      8   /* BiCGSTABSolver::solve                   */
 #define BTM_PHASE_AMGPCG        9   /* AMG-preconditioned CG                   */
-#define BTM_PHASE_ITER         10   /* ---- served request loop with continuous batching -------------------------
+#define BTM_PHASE_ITER         10   /* Mesh::computeWallDistance (core/src/Mesh.cpp:345-373) on the device:
+ * out[c] = min over the wall face centres of |cell_centre[c] - w| (xyz
+ * triples), 1e10 when there is no wall face; bit-identical to the reference.
+ * Host buffers in and out. */
+int btm_wall_distance(int32_t n_cells, const double *cell_centre, int32_t n_wall, const double *wall_centre,
+                      double *out);
+
+/* ---- served request loop with continuous batching -------------------------
  *
  * No single reference counterpart: it replaces the calibration layer's
  * pattern of issuing ForwardModel::evaluate calls from many MCMC chains /
