@@ -17,8 +17,9 @@ from ._observe import ObservationOperator
 from ._forward import ForwardModel, SolveOutput, solve, solve_batch
 from ._lib import Case, BtmError, library_path
 from ._server import Server
+from ._sensitivity import ParameterSensitivity, TangentGradientResult
 
 __all__ = ["Mesh", "BCType", "EvaluationResult", "EvaluationStatus", "FlowBoundaryConditions",
            "InferenceParameterSet", "PatchBC", "SolverSettings", "SSTCoefficients", "Vec3",
            "ObservationOperator", "ForwardModel", "SolveOutput", "solve", "solve_batch", "Case",
-           "BtmError", "library_path", "Server"]
+           "BtmError", "library_path", "Server", "ParameterSensitivity", "TangentGradientResult"]
