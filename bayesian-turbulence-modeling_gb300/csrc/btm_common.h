@@ -9,6 +9,12 @@ namespace btm {
 
 constexpr int kMaxLevels = 20;       // AMG levels (reference cap, LinearSolver.hpp:508)
 constexpr int kCoarseDirect = 32;    // coarsest level at or below this size: dense inverse
+// Meshes that run on the cooperative grid stop coarsening at this size: the
+// Galerkin levels of the strength-0.25 aggregation shrink by only a few per
+// cent a level below ~1000 rows (a 120k-cell step mesh reaches the 20-level
+// cap at ~530 rows), and each level costs the V-cycle ~27 dependent phases on
+// one CTA, while a dense inverse of this size is one grid-wide mat-vec.
+constexpr int kCoarseDirectGrid = 1024;
 constexpr int kCoarseSweeps = 50;    // GS sweeps when the coarsest level is larger
 constexpr int kRedSlots = 4;         // values per fused team reduction
 

@@ -197,7 +197,21 @@ template <class T>
 __device__ void amg_coarse_solve(T &tm, const DevMesh &M, DevInst &I) {
     const int l = M.nLevels - 1;
     const int n = M.lev[l].n;
-    if (M.coarseDirect) {
+    if (M.coarseDirect && n > kCoarseDirect) {
+        // grid-size dense inverse: one warp per row, lane-strided partial
+        // sums folded by a butterfly
+        const double *b = lev_b(I, M, l);
+        double *x = lev_x(I, M, l);
+        const int lane = tm.rank() & 31;
+        for (int i = tm.rank() >> 5; i < n; i += tm.size() >> 5) {
+            const double *row = I.ainv + (size_t)i * n;
+            double s = 0.0;
+            for (int j = lane; j < n; j += 32) s = fma(LD(row + j), LD(b + j), s);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) x[i] = s;
+        }
+        tm.sync();
+    } else if (M.coarseDirect) {
         const double *b = lev_b(I, M, l);
         double *x = lev_x(I, M, l);
         for (int i = tm.rank(); i < n; i += tm.size()) {
@@ -211,30 +225,61 @@ __device__ void amg_coarse_solve(T &tm, const DevMesh &M, DevInst &I) {
     }
 }
 
-// V-cycle on levels [l0, nLevels): 2 pre-sweeps (colours ascending), 2 post
-// sweeps (colours descending) so the preconditioner is symmetric.
+// one damped-Jacobi sweep on a coarse level (l >= 1): reads x, writes `out`
+constexpr double kJacobiWeight64 = 0.7;
+template <class T>
+__device__ __noinline__ void amg_jacobi(T &tm, const DevMesh &M, DevInst &I, int l, const double *x, double *out) {
+    const AmgLevelDev &L = M.lev[l];
+    const double *b = lev_b(I, M, l), *val = lev_vals(I, M, l), *rd = lev_rd(I, M, l);
+    for (int i = tm.rank(); i < L.n; i += tm.size()) {
+        double s = LD(b + i);
+        for (int q = L.rowPtr[i]; q < L.rowPtr[i + 1]; ++q) s = fma(-LD(val + q), LD(x + L.colIdx[q]), s);
+        out[i] = fma(kJacobiWeight64 * LD(rd + i), s, LD(x + i));
+    }
+    tm.sync();
+}
+
+// Two smoothing sweeps of level l: multicolour Gauss-Seidel (colours
+// ascending before the coarse correction, descending after).  On the
+// cooperative grid the coarse levels take a pair of damped-Jacobi sweeps
+// (x -> r -> x) instead: one grid barrier per sweep rather than one per
+// colour (6-11 colours on Galerkin levels), for ~15-20 % more PCG iterations.
+template <class T> struct GridSmoothing { static constexpr bool jacobi = false; };
+template <> struct GridSmoothing<GridTeam> { static constexpr bool jacobi = true; };
+
+template <class T>
+__device__ void amg_smooth2(T &tm, const DevMesh &M, DevInst &I, int l, bool post) {
+    if (l == 0 || !GridSmoothing<T>::jacobi) {
+        amg_gs_sweep(tm, M, I, l, post);
+        amg_gs_sweep(tm, M, I, l, post);
+    } else {
+        double *x = lev_x(I, M, l), *tmp = lev_r(I, M, l);
+        amg_jacobi(tm, M, I, l, x, tmp);
+        amg_jacobi(tm, M, I, l, tmp, x);
+    }
+}
+
+// V-cycle on levels [l0, nLevels): 2 pre-sweeps, 2 post sweeps, symmetric so
+// the preconditioner suits CG.
 template <class T>
 __device__ void amg_vcycle_from(T &tm, const DevMesh &M, DevInst &I, int l0) {
     const int nl = M.nLevels;
     for (int l = l0; l < nl - 1; ++l) {
-        amg_gs_sweep(tm, M, I, l, false);
-        amg_gs_sweep(tm, M, I, l, false);
+        amg_smooth2(tm, M, I, l, false);
         amg_restrict(tm, M, I, l);
     }
     amg_coarse_solve(tm, M, I);
     for (int l = nl - 2; l >= l0; --l) {
         amg_prolong(tm, M, I, l);
-        amg_gs_sweep(tm, M, I, l, true);
-        amg_gs_sweep(tm, M, I, l, true);
+        amg_smooth2(tm, M, I, l, true);
     }
 }
 
-// Levels below this size run on CTA 0 alone in grid mode.
-constexpr int kSmallLevel = 16384;
-
-template <class T> struct AmgDriver;
-template <> struct AmgDriver<BlockTeam> {
-    __device__ static void setup(BlockTeam &tm, const DevMesh &M, DevInst &I) {
+// Hierarchy refresh and V-cycle, the same on one CTA and on the cooperative
+// grid (every level on the whole team; the grid's dense coarsest level has
+// up to kCoarseDirectGrid rows and is inverted and applied by all CTAs).
+template <class T> struct AmgDriver {
+    __device__ static void setup(T &tm, const DevMesh &M, DevInst &I) {
         amg_level_rd(tm, M, I, 0);
         for (int l = 1; l < M.nLevels; ++l) {
             amg_galerkin(tm, M, I, l);
@@ -244,54 +289,8 @@ template <> struct AmgDriver<BlockTeam> {
         tm.sync();
         if (M.coarseDirect) amg_coarse_inverse(tm, M, I);
     }
-    __device__ static void vcycle(BlockTeam &tm, const DevMesh &M, DevInst &I) {
+    __device__ static void vcycle(T &tm, const DevMesh &M, DevInst &I) {
         amg_vcycle_from(tm, M, I, 0);
-    }
-};
-template <> struct AmgDriver<GridTeam> {
-    __device__ static int split(const DevMesh &M) {
-        int l = 0;
-        while (l < M.nLevels - 1 && M.lev[l].n >= kSmallLevel) ++l;
-        return l;
-    }
-    __device__ static void setup(GridTeam &tm, const DevMesh &M, DevInst &I) {
-        const int ls = split(M);
-        amg_level_rd(tm, M, I, 0);
-        for (int l = 1; l <= ls && l < M.nLevels; ++l) {
-            amg_galerkin(tm, M, I, l);
-            tm.sync();
-            amg_level_rd(tm, M, I, l);
-        }
-        tm.sync();
-        if (blockIdx.x == 0) {
-            BlockTeamCG bt{{tm.red, tm.buf}};
-            for (int l = ls + 1; l < M.nLevels; ++l) {
-                amg_galerkin(bt, M, I, l);
-                bt.sync();
-                amg_level_rd(bt, M, I, l);
-            }
-            bt.sync();
-            if (M.coarseDirect) amg_coarse_inverse(bt, M, I);
-        }
-        tm.sync();
-    }
-    __device__ static void vcycle(GridTeam &tm, const DevMesh &M, DevInst &I) {
-        const int ls = split(M);
-        for (int l = 0; l < ls; ++l) {
-            amg_gs_sweep(tm, M, I, l, false);
-            amg_gs_sweep(tm, M, I, l, false);
-            amg_restrict(tm, M, I, l);
-        }
-        if (blockIdx.x == 0) {
-            BlockTeamCG bt{{tm.red, tm.buf}};
-            amg_vcycle_from(bt, M, I, ls);
-        }
-        tm.sync();
-        for (int l = ls - 1; l >= 0; --l) {
-            amg_prolong(tm, M, I, l);
-            amg_gs_sweep(tm, M, I, l, true);
-            amg_gs_sweep(tm, M, I, l, true);
-        }
     }
 };
 

@@ -124,6 +124,59 @@ int aggregate(const HLevel &L, std::vector<int> &map) {
     return nCoarse;
 }
 
+// Plain aggregation with a row-relative strength measure, for levels where
+// the reference rule stalls (see build_case).  a_ij is strong when
+// |a_ij| > 0.25 max_k!=i |a_ik|, so every row has a strong neighbour.  Pass 1
+// seeds an aggregate at i with its strong neighbours only when none of them
+// is aggregated yet (the reference rule seeds every unaggregated row, which
+// on Galerkin levels of a stretched 3-D mesh leaves ~97 % singletons); pass 2
+// joins each remaining row to its strongest aggregated neighbour (decided on
+// the pass-1 aggregates only); pass 3 groups what is left with its
+// unaggregated strong neighbours.
+int aggregate_plain(const HLevel &L, std::vector<int> &map) {
+    const int n = L.n;
+    map.assign(n, -1);
+    std::vector<double> rmax(n, 0.0);
+    for (int i = 0; i < n; ++i)
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j)
+            if (L.colIdx[j] != i) rmax[i] = std::max(rmax[i], std::abs(L.val[j]));
+    auto strong = [&](int i, int j) { return L.colIdx[j] != i && std::abs(L.val[j]) > 0.25 * rmax[i]; };
+    int nCoarse = 0;
+    for (int i = 0; i < n; ++i) {
+        if (map[i] >= 0) continue;
+        bool seed = true;
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1] && seed; ++j)
+            if (strong(i, j) && map[L.colIdx[j]] >= 0) seed = false;
+        if (!seed) continue;
+        const int agg = nCoarse++;
+        map[i] = agg;
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j)
+            if (strong(i, j)) map[L.colIdx[j]] = agg;
+    }
+    std::vector<int> join(n, -1);
+    for (int i = 0; i < n; ++i) {
+        if (map[i] >= 0) continue;
+        double best = -1.0;
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j) {
+            const int c = L.colIdx[j];
+            if (c != i && map[c] >= 0 && std::abs(L.val[j]) > best) {
+                best = std::abs(L.val[j]);
+                join[i] = map[c];
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        if (join[i] >= 0) map[i] = join[i];
+    for (int i = 0; i < n; ++i) {
+        if (map[i] >= 0) continue;
+        const int agg = nCoarse++;
+        map[i] = agg;
+        for (int j = L.rowPtr[i]; j < L.rowPtr[i + 1]; ++j)
+            if (strong(i, j) && map[L.colIdx[j]] < 0) map[L.colIdx[j]] = agg;
+    }
+    return nCoarse;
+}
+
 // Galerkin product A_c = P^T A P for piecewise-constant P: builds the coarse
 // CSR, its geometric values and, per coarse entry, the list of fine entry ids
 // that sum into it (members ascending, then fine columns ascending).
@@ -233,6 +286,7 @@ void colour(HLevel &L) {
 }  // namespace
 
 namespace {
+int block_max_cells();
 
 std::once_flag g_dev_once;
 int g_dev_status = 0;
@@ -478,9 +532,19 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
             }
         }
     }
-    while ((int)lv.size() < btm::kMaxLevels && lv.back().n > btm::kCoarseDirect) {
+    // cooperative-grid meshes keep a dense coarsest level of up to
+    // kCoarseDirectGrid rows (level 0 is always coarsened once)
+    const int directMax = nC > block_max_cells() ? btm::kCoarseDirectGrid : btm::kCoarseDirect;
+    while ((int)lv.size() < btm::kMaxLevels && lv.back().n > btm::kCoarseDirect &&
+           (lv.size() == 1 || lv.back().n > directMax)) {
         HLevel &F = lv.back();
         int nc = aggregate(F, F.map);
+        // On cooperative-grid meshes a level that the reference rule shrinks
+        // by less than 20 % is aggregated by aggregate_plain instead: on a
+        // stretched 3-D duct the reference rule stalls at ~18 % of the fine
+        // size and fills the 20-level cap with near-identical levels, each
+        // costing a full set of grid-wide sweeps.
+        if (directMax > btm::kCoarseDirect && nc > 0.8 * F.n) nc = aggregate_plain(F, F.map);
         if (nc == 0 || nc >= F.n) { F.map.clear(); break; }
         F.nCoarse = nc;
         HLevel Cl;
@@ -490,7 +554,7 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
     for (auto &L : lv) colour(L);
     const int nL = (int)lv.size();
     D.nLevels = nL;
-    D.coarseDirect = lv.back().n <= btm::kCoarseDirect ? 1 : 0;
+    D.coarseDirect = lv.back().n <= directMax ? 1 : 0;
     C->amgCoarseN = lv.back().n;
 
     // ---- index validation: every gather index the kernels use is checked

@@ -791,7 +791,21 @@ template <class T>
 __device__ void mx_amg_coarse_solve(T &tm, const DevMesh &M, DevWork32 &F) {
     const int l = M.nLevels - 1;
     const int n = M.lev[l].n;
-    if (M.coarseDirect) {
+    if (M.coarseDirect && n > kCoarseDirect) {
+        // grid-size dense inverse: one warp per row, lane-strided partial
+        // sums folded by a butterfly
+        const float *b = lev_bf(F, M, l);
+        float *x = lev_xf(F, M, l);
+        const int lane = tm.rank() & 31;
+        for (int i = tm.rank() >> 5; i < n; i += tm.size() >> 5) {
+            const double *row = F.ainv + (size_t)i * n;
+            double s = 0.0;
+            for (int j = lane; j < n; j += 32) s = fma(LD(row + j), (double)LD(b + j), s);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) x[i] = (float)s;
+        }
+        tm.sync();
+    } else if (M.coarseDirect) {
         const float *b = lev_bf(F, M, l);
         float *x = lev_xf(F, M, l);
         for (int i = tm.rank(); i < n; i += tm.size()) {
@@ -822,12 +836,12 @@ __device__ void mx_amg_values_from(T &tm, const DevMesh &M, DevWork32 &F, int l0
 // ascending), 2 post-sweeps (colours descending)
 // two smoothing sweeps of level l: multicolour Gauss-Seidel (colours
 // ascending before the coarse correction, descending after); on the coarse
-// levels of a one-CTA instance a pair of damped-Jacobi sweeps (x -> r -> x)
-// instead, which needs no colour barriers and cost ~20 % more PCG iterations
-// on 2-D meshes (on a 3-D 2M-cell duct it cost 30x: grid-mode instances keep
-// Gauss-Seidel)
+// levels a pair of damped-Jacobi sweeps (x -> r -> x) instead, which needs
+// one barrier per sweep rather than one per colour (6-11 colours on Galerkin
+// levels) and costs ~15-20 % more PCG iterations
 template <class T> struct CoarseJacobi { static constexpr bool value = false; };
 template <> struct CoarseJacobi<BlockTeam> { static constexpr bool value = true; };
+template <> struct CoarseJacobi<GridTeam> { static constexpr bool value = true; };
 
 template <class T>
 __device__ void mx_amg_smooth2(T &tm, const DevMesh &M, DevWork32 &F, int l, bool post) {
@@ -859,9 +873,10 @@ __device__ void mx_amg_vcycle_from(T &tm, const DevMesh &M, DevWork32 &F, int l0
 // refreshed when `coarse` is set and otherwise kept from an earlier outer
 // iteration: a Galerkin hierarchy of an earlier SPD pressure matrix is still
 // an SPD preconditioner for the current one, and level 0 always smooths with
-// the current matrix.  Every level runs on the whole team: on the coarse
-// levels a single warp's dependent latency chain cost more than the barriers
-// it saved.
+// the current matrix.  Every level runs on the whole team (one CTA, or the
+// cooperative grid): on the coarse levels a single warp's dependent latency
+// chain cost more than the barriers it saved, and on the grid the coarse
+// levels held by CTA 0 alone cost 2-3x a grid-wide Jacobi level.
 template <class T>
 __device__ void mx_amg_setup(T &tm, const DevMesh &M, DevWork32 &F, bool coarse = true) {
     mx_amg_level_rd(tm, M, F, 0);
@@ -874,53 +889,6 @@ __device__ void mx_amg_setup(T &tm, const DevMesh &M, DevWork32 &F, bool coarse 
 template <class T>
 __device__ void mx_amg_vcycle(T &tm, const DevMesh &M, DevWork32 &F) {
     mx_amg_vcycle_from(tm, M, F, 0);
-}
-
-// Grid-team setup and V-cycle (meshes above the one-CTA size): levels of at
-// least kGridLevelRows rows run on the whole cooperative grid, the coarser
-// ones on CTA 0 alone (its loads bypass L1 like the grid's).
-constexpr int kGridLevelRows = 16384;
-
-__device__ __forceinline__ int mx_grid_split(const DevMesh &M) {
-    int l = 0;
-    while (l < M.nLevels - 1 && M.lev[l].n >= kGridLevelRows) ++l;
-    return l;
-}
-
-__device__ void mx_amg_setup(GridTeam &tm, const DevMesh &M, DevWork32 &F, bool coarse = true) {
-    const int ls = mx_grid_split(M);
-    mx_amg_level_rd(tm, M, F, 0);
-    tm.sync();
-    if (!coarse) return;
-    for (int l = 1; l <= ls && l < M.nLevels; ++l) {
-        mx_amg_galerkin(tm, M, F, l);
-        tm.sync();
-        mx_amg_level_rd(tm, M, F, l);
-        tm.sync();
-    }
-    if (blockIdx.x == 0) {
-        BlockTeamCG bt{{tm.red, tm.buf}};
-        mx_amg_values_from(bt, M, F, ls + 1);
-        if (M.coarseDirect) mx_amg_coarse_inverse(bt, M, F);
-    }
-    tm.sync();
-}
-
-__device__ void mx_amg_vcycle(GridTeam &tm, const DevMesh &M, DevWork32 &F) {
-    const int ls = mx_grid_split(M);
-    for (int l = 0; l < ls; ++l) {
-        mx_amg_smooth2(tm, M, F, l, false);
-        mx_amg_restrict(tm, M, F, l);
-    }
-    if (blockIdx.x == 0) {
-        BlockTeamCG bt{{tm.red, tm.buf}};
-        mx_amg_vcycle_from(bt, M, F, ls);
-    }
-    tm.sync();
-    for (int l = ls - 1; l >= 0; --l) {
-        mx_amg_prolong(tm, M, F, l);
-        mx_amg_smooth2(tm, M, F, l, true);
-    }
 }
 
 // AMG-preconditioned CG (AMGSolver::solve, LinearSolver.hpp:602-653):

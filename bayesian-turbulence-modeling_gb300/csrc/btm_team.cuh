@@ -1,7 +1,7 @@
 // btm_team.cuh - execution teams shared by the FP64 and mixed-precision
-// engines: one CTA (BlockTeam), a whole cooperative grid (GridTeam) or CTA 0
-// inside a grid (BlockTeamCG); deterministic fixed-order team reductions and
-// a bounded software grid barrier.  Header-only device code.
+// engines: one CTA (BlockTeam) or a whole cooperative grid (GridTeam);
+// deterministic fixed-order team reductions and a bounded software grid
+// barrier.  Header-only device code.
 #pragma once
 #include "btm_common.h"
 
@@ -302,10 +302,6 @@ struct GridTeam {
     }
 };
 
-// CTA 0 working alone inside a grid launch (coarse AMG levels): same as a
-// BlockTeam but its loads bypass L1 like the grid team's.
-struct BlockTeamCG : BlockTeam {};
-
 // Loads that must see writes made by other CTAs in the same launch (after a
 // grid barrier) bypass L1: in grid mode every field read goes through __ldcg.
 // In block mode one CTA owns the data and plain loads are coherent.
@@ -315,10 +311,6 @@ template <> struct Ld<BlockTeam> {
     __device__ __forceinline__ static float f(const float *p) { return *p; }
 };
 template <> struct Ld<GridTeam> {
-    __device__ __forceinline__ static double f(const double *p) { return __ldcg(p); }
-    __device__ __forceinline__ static float f(const float *p) { return __ldcg(p); }
-};
-template <> struct Ld<BlockTeamCG> {
     __device__ __forceinline__ static double f(const double *p) { return __ldcg(p); }
     __device__ __forceinline__ static float f(const float *p) { return __ldcg(p); }
 };

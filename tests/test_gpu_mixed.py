@@ -128,29 +128,41 @@ from rans_sst_py import FlowBoundaryConditions, Case, solve
 from rans_sst_py._lib import lib
 g = cases.load_golden("chan180_4x32")
 m = cases.mesh_from_bytes(bytes(g["mesh"])); m.compute_wall_distance()
-s = cases.channel_settings(20000, 1e-8); s.precision = "mixed"
-case = Case(m, FlowBoundaryConditions.channel_defaults(m, 0, 0, 0), float(g["nu"]), s)
 a = g["init"]
-out = solve(case, cases.COEFF_DEFAULTS, 0, dict(u=tuple(a[:3]), p=float(a[3]), k=float(a[4]), omega=float(a[5])))
-print(json.dumps(dict(converged=out.converged, err={{f: cases.rel_l2(out.state[f], g["stag_" + f])
-                                                   for f in ("U", "k", "omega", "nuT")}})))
+ini = dict(u=tuple(a[:3]), p=float(a[3]), k=float(a[4]), omega=float(a[5]))
+res = {{}}
+for name, it, tol in (("conv", 20000, 1e-8), ("stag", int(g["stag_iterations_run"]), 0.0)):
+    if name == "stag" and {precision!r} != "fp64":
+        continue
+    s = cases.channel_settings(it, tol); s.precision = {precision!r}
+    case = Case(m, FlowBoundaryConditions.channel_defaults(m, 0, 0, 0), float(g["nu"]), s)
+    out = solve(case, cases.COEFF_DEFAULTS, 0, ini)
+    res[name] = dict(converged=out.converged, iterations=out.iterations_run,
+                     err={{f: cases.rel_l2(out.state[f], g["stag_" + f]) for f in ("U", "k", "omega", "nuT")}})
+print(json.dumps(res))
 """
 
 
-def test_mixed_grid_mode_converges_to_reference():
-    """Meshes above the one-CTA size run the mixed engine over a cooperative
-    grid.  Forced onto the grid path (BTM_BLOCK_MAX_CELLS below the mesh size,
-    in a child process: the limit is read once per process), the Re_tau = 180
-    channel converges to the reference's stagnated fields within 1e-6."""
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_grid_mode_converges_to_reference(precision):
+    """Meshes above the one-CTA size run over a cooperative grid, with a dense
+    coarsest AMG level of up to 1024 rows solved by the whole grid.  Forced
+    onto the grid path (BTM_BLOCK_MAX_CELLS below the mesh size, in a child
+    process: the limit is read once per process), the Re_tau = 180 channel
+    converges to the reference's stagnated fields within 1e-6, and the FP64
+    engine run to the reference's stagnation count matches them within 1e-8."""
     import json
     import os
     import subprocess
     import sys
     paths = [os.path.dirname(os.path.abspath(__file__)), cases.ROOT, cases.PKG]
     env = dict(os.environ, BTM_BLOCK_MAX_CELLS="64")
-    r = subprocess.run([sys.executable, "-c", GRID_SCRIPT.format(paths=paths)], env=env, capture_output=True,
-                       text=True, timeout=600)
+    r = subprocess.run([sys.executable, "-c", GRID_SCRIPT.format(paths=paths, precision=precision)], env=env,
+                       capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     res = json.loads(r.stdout.strip().splitlines()[-1])
-    assert res["converged"]
-    _check(res["err"])
+    assert res["conv"]["converged"]
+    _check(res["conv"]["err"])
+    if precision == "fp64":
+        for f, e in res["stag"]["err"].items():
+            assert e <= 1e-8, (f, e)
