@@ -49,6 +49,26 @@ struct DevGeom32 {
     const float *vol, *rvol, *wd;                                   // [nC]; rvol = 1/V (1 if V <= 1e-30)
 };
 
+// Observation operator of a case (ObservationOperator.hpp:46-378), resolved
+// on the host: per observable its kind (BTM_OBS_*), the cell or the range of
+// listed wall faces it reads, and the constants of its formula; per listed
+// face (patch order) what the wall-shear formulas read.
+struct ObsDev {
+    int32_t n;                 // observables (0: none)
+    const int32_t *kind;       // [n] BTM_OBS_*
+    const int32_t *at;         // [n] cell (probe, tap), first listed face (patch kinds)
+    const int32_t *cnt;        // [n] listed faces (patch kinds)
+    const int32_t *comp;       // [n] velocity component
+    const double *observed;    // [n]
+    const double *var;         // [n] sigma_obs^2 + sigma_model^2, floored at 1e-30
+    const double *c0;          // [n] denominator: q_ref A (drag), max(q_ref, 1e-20) (tap, Cf)
+    const double *c1;          // [n] p_ref (tap), x of the last patch face (reattachment default)
+    // listed faces
+    const int32_t *fOwn, *fBnd;            // owner cell, boundary index
+    const double *fNx, *fNy, *fNz;         // unit normal
+    const double *fArea, *fDelta, *fX;     // area, max(delta, 1e-20), face-centre x
+};
+
 struct DevMesh {
     int32_t nC, nIF, nB, nF;
     int32_t is2d;          // all normals z == 0: the z-momentum system is identically zero
@@ -87,6 +107,7 @@ struct DevMesh {
     AmgLevelDev lev[kMaxLevels];
     int64_t amgValTotal, amgVecTotal;
     DevGeom32 g32;
+    ObsDev obs;
 };
 
 // Scalar controls of one solve (SolverSettings fields read by the loop).
@@ -164,6 +185,9 @@ struct DevInst {
     double *dbgIn, *dbgOut;
     // mixed-precision bulk (null for the FP64 engine)
     DevWork32 f;
+    // observation outputs [obs.n + 1]: predictions, then the log-likelihood
+    // (null: not evaluated)
+    double *obsOut;
     // served requests: completion flag in mapped host memory (null otherwise),
     // set by the leader after every output is written
     volatile int32_t *doneFlag;

@@ -20,6 +20,7 @@
 #include "btm_team.cuh"
 #include "btm_bc.cuh"
 #include "btm_phases64.cuh"
+#include "btm_observe.cuh"
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -666,6 +667,7 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
         for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
         I.outTime[8] = tStart;
         I.outTime[9] = globaltimer_ns();
+        if (I.obsOut) observe_leader<T>(M, I);
         if (I.doneFlag) {
             __threadfence_system();
             *I.doneFlag = 1;

@@ -780,8 +780,44 @@ void ensure_mixed(btm_case *C, Slab &S) {
     if ((size_t)((char *)d - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "fp32 slab overflow");
 }
 
+// Observation outputs [n_obs + 1] of a slab, allocated on the first solve
+// that asks for predictions.
+void ensure_obs(btm_case *C, Slab &S, bool want) {
+    const int n = C->dmesh.obs.n;
+    if (!want || n == 0) {
+        S.inst.obsOut = nullptr;
+        return;
+    }
+    if (S.obsCap < n + 1) {
+        if (S.dObs) cudaFree(S.dObs);
+        S.dObs = nullptr;
+        S.obsCap = 0;
+        ck(cudaMalloc((void **)&S.dObs, sizeof(double) * (n + 1)), "cudaMalloc(observations)");
+        S.obsCap = n + 1;
+    }
+    S.inst.obsOut = S.dObs;
+}
+
+void download_obs(btm_case *C, const btm::DevInst &I, btm_history *h, cudaStream_t st) {
+    if (!I.obsOut || !h || !h->predictions) return;
+    const int n = C->dmesh.obs.n;
+    std::vector<double> v(n + 1);
+    ck(cudaMemcpyAsync(v.data(), I.obsOut, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, st), "observations");
+    ck(cudaStreamSynchronize(st), "observations");
+    for (int k = 0; k < n; ++k) h->predictions[k] = v[k];
+    h->log_lik = v[n];
+}
+
+void free_slab(Slab &S) {
+    if (S.dptr) cudaFree(S.dptr);
+    if (S.dptr32) cudaFree(S.dptr32);
+    if (S.dObs) cudaFree(S.dObs);
+    S = Slab();
+}
+
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
     I.S = dev_settings(C->settings);
+    I.obsOut = nullptr;
     I.nu = C->nu;
     for (int q = 0; q < 11; ++q) I.coeff[q] = coeffs[q];
     I.variant = variant;
@@ -912,11 +948,9 @@ int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu, co
 
 void btm_case_destroy(btm_case *C) {
     if (!C) return;
-    for (Slab &s : C->slabs) {
-        if (s.dptr) cudaFree(s.dptr);
-        if (s.dptr32) cudaFree(s.dptr32);
-    }
+    for (Slab &s : C->slabs) free_slab(s);
     if (C->meshArena) cudaFree(C->meshArena);
+    if (C->obsArena) cudaFree(C->obsArena);
     if (C->dMeshPtr) cudaFree(C->dMeshPtr);
     if (C->stream) cudaStreamDestroy(C->stream);
     delete C;
@@ -946,6 +980,140 @@ int btm_case_set_settings(btm_case *C, const btm_settings *s) {
         if (e != cudaSuccess) return fail(BTM_ERR_CUDA, cudaGetErrorString(e));
     }
     C->settings = *s;
+    return BTM_OK;
+}
+
+// ObservationOperator::evaluate's searches and constants
+// (core/include/ObservationOperator.hpp:159-364), resolved once per case:
+// nearest cell / nearest patch face by squared distance, first minimum wins;
+// q_ref = 0.5 U_ref^2 (times rho for a tap); wall distances floored at 1e-20.
+int btm_case_set_observations(btm_case *C, const btm_mesh *m, int32_t n, const btm_observable *obs) {
+    if (!C || n < 0 || (n > 0 && (!m || !obs))) return fail(BTM_ERR_ARG, "null argument");
+    try {
+        btm::ObsDev O{};
+        void *arena = nullptr;
+        if (n > 0) {
+            if (m->n_cells != C->nC || m->n_faces != C->nF || m->n_internal_faces != C->nIF)
+                throw BtmError(BTM_ERR_ARG, "btm_case_set_observations: mesh does not match the case");
+            const int nIF = m->n_internal_faces;
+            std::vector<int32_t> kind(n), at(n), cnt(n), comp(n);
+            std::vector<double> observed(n), var(n), c0(n, 1.0), c1(n, 0.0);
+            std::vector<int32_t> fOwn, fBnd;
+            std::vector<double> fNx, fNy, fNz, fArea, fDelta, fX;
+            auto list_face = [&](int f) {
+                fOwn.push_back(m->owner[f]);
+                fBnd.push_back(f - nIF);
+                fNx.push_back(m->face_normal[3 * f]);
+                fNy.push_back(m->face_normal[3 * f + 1]);
+                fNz.push_back(m->face_normal[3 * f + 2]);
+                fArea.push_back(m->face_area[f]);
+                fDelta.push_back(std::max(m->face_delta[f], 1e-20));
+                fX.push_back(m->face_center[3 * f]);
+            };
+            auto dist2 = [](const double *c, const double *loc) {
+                const double d0 = c[0] - loc[0], d1 = c[1] - loc[1], d2 = c[2] - loc[2];
+                const double a = d0 * d0, b = d1 * d1, e = d2 * d2;
+                return (a + b) + e;
+            };
+            for (int k = 0; k < n; ++k) {
+                const btm_observable &o = obs[k];
+                if (o.type < BTM_OBS_DRAG || o.type > BTM_OBS_REATTACHMENT)
+                    throw BtmError(BTM_ERR_ARG, "btm_case_set_observations: unknown observable type");
+                kind[k] = o.type;
+                observed[k] = o.observed;
+                const double so = o.sigma_obs * o.sigma_obs, sm = o.sigma_model * o.sigma_model;
+                var[k] = so + sm;
+                if (var[k] < 1e-30) var[k] = 1e-30;
+                comp[k] = o.component == 0 ? 0 : (o.component == 1 ? 1 : 2);
+                const double qref = (0.5 * o.ref_velocity) * o.ref_velocity;
+                if (o.type == BTM_OBS_PRESSURE_TAP || o.type == BTM_OBS_VELOCITY) {
+                    int best = 0;
+                    double bd = 0.0;
+                    for (int c = 0; c < m->n_cells; ++c) {
+                        const double d = dist2(m->cell_center + 3 * c, o.location);
+                        if (c == 0 || d < bd) { bd = d; best = c; }
+                    }
+                    at[k] = best;
+                    cnt[k] = 0;
+                    if (o.type == BTM_OBS_PRESSURE_TAP) {
+                        const double q = ((0.5 * o.ref_density) * o.ref_velocity) * o.ref_velocity;
+                        c0[k] = std::max(q, 1e-20);
+                        c1[k] = o.ref_pressure;
+                    }
+                    continue;
+                }
+                if (o.patch < 0 || o.patch >= m->n_patches)
+                    throw BtmError(BTM_ERR_ARG, "btm_case_set_observations: patch index out of range");
+                const int p0 = m->patch_offset[o.patch], p1 = m->patch_offset[o.patch + 1];
+                for (int q = p0; q < p1; ++q)
+                    if (m->patch_faces[q] < nIF || m->patch_faces[q] >= m->n_faces)
+                        throw BtmError(BTM_ERR_ARG, "btm_case_set_observations: patch face is not a boundary face");
+                at[k] = (int)fOwn.size();
+                if (o.type == BTM_OBS_SKIN_FRICTION) {
+                    cnt[k] = p1 > p0 ? 1 : 0;
+                    c0[k] = std::max(qref, 1e-20);
+                    if (p1 > p0) {
+                        int best = p0;
+                        double bd = 0.0;
+                        for (int q = p0; q < p1; ++q) {
+                            const double d = dist2(m->face_center + 3 * m->patch_faces[q], o.location);
+                            if (q == p0 || d < bd) { bd = d; best = q; }
+                        }
+                        list_face(m->patch_faces[best]);
+                    }
+                    continue;
+                }
+                cnt[k] = p1 - p0;
+                for (int q = p0; q < p1; ++q) list_face(m->patch_faces[q]);
+                if (o.type == BTM_OBS_DRAG) c0[k] = qref * o.ref_area;
+                if (o.type == BTM_OBS_REATTACHMENT) c1[k] = p1 > p0 ? m->face_center[3 * m->patch_faces[p1 - 1]] : 0.0;
+            }
+            const size_t nf = std::max<size_t>(fOwn.size(), 1);
+            const size_t al = 32;  // doubles: 256-byte alignment
+            auto up = [&](size_t x) { return (x + al - 1) & ~(al - 1); };
+            const size_t words = 4 * up(n) + 4 * up(n) + 2 * up(nf) + 6 * up(nf);
+            ck(cudaMalloc(&arena, words * 8), "cudaMalloc(observation plan)");
+            char *d = (char *)arena;
+            auto put = [&](const void *src, size_t bytes, size_t cap) {
+                char *p = d;
+                if (bytes) ck(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice), "cudaMemcpy(observation plan)");
+                d += cap * 8;
+                return (void *)p;
+            };
+            O.n = n;
+            O.kind = (const int32_t *)put(kind.data(), 4 * n, up(n));
+            O.at = (const int32_t *)put(at.data(), 4 * n, up(n));
+            O.cnt = (const int32_t *)put(cnt.data(), 4 * n, up(n));
+            O.comp = (const int32_t *)put(comp.data(), 4 * n, up(n));
+            O.observed = (const double *)put(observed.data(), 8 * n, up(n));
+            O.var = (const double *)put(var.data(), 8 * n, up(n));
+            O.c0 = (const double *)put(c0.data(), 8 * n, up(n));
+            O.c1 = (const double *)put(c1.data(), 8 * n, up(n));
+            O.fOwn = (const int32_t *)put(fOwn.data(), 4 * fOwn.size(), up(nf));
+            O.fBnd = (const int32_t *)put(fBnd.data(), 4 * fBnd.size(), up(nf));
+            O.fNx = (const double *)put(fNx.data(), 8 * fNx.size(), up(nf));
+            O.fNy = (const double *)put(fNy.data(), 8 * fNy.size(), up(nf));
+            O.fNz = (const double *)put(fNz.data(), 8 * fNz.size(), up(nf));
+            O.fArea = (const double *)put(fArea.data(), 8 * fArea.size(), up(nf));
+            O.fDelta = (const double *)put(fDelta.data(), 8 * fDelta.size(), up(nf));
+            O.fX = (const double *)put(fX.data(), 8 * fX.size(), up(nf));
+            if ((size_t)(d - (char *)arena) > words * 8) throw BtmError(BTM_ERR_INTERNAL, "observation plan overflow");
+        }
+        btm::DevMesh D = C->dmesh;
+        D.obs = O;
+        cudaError_t e = cudaMemcpy(C->dMeshPtr, &D, sizeof D, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            if (arena) cudaFree(arena);
+            throw BtmError(BTM_ERR_CUDA, cudaGetErrorString(e));
+        }
+        if (C->obsArena) cudaFree(C->obsArena);
+        C->obsArena = arena;
+        C->dmesh = D;
+    } catch (const BtmError &e) {
+        return fail(e.code, e.what());
+    } catch (const std::exception &e) {
+        return fail(BTM_ERR_INTERNAL, e.what());
+    }
     return BTM_OK;
 }
 
@@ -1002,6 +1170,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             ck(cudaMemsetAsync(I.barrier, 0, 512, st), "memset control");
             const bool mixed = J.C->settings.precision == BTM_PREC_MIXED;
             if (mixed) ensure_mixed(J.C, *J.S);
+            ensure_obs(J.C, *J.S, hists && hists[i].predictions);
             if (mixed && J.C->nC <= block_max_cells()) {
                 mixIdx.push_back(i);
             } else if (!mixed && J.C->nC <= block_max_cells()) {
@@ -1110,6 +1279,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                     ck(cudaMemcpy(h.residuals, histDev[i], sizeof(double) * 6 * rows, cudaMemcpyDeviceToHost), "hist");
                     cudaFree(histDev[i]);
                 }
+                download_obs(J.C, I, &h, st);
             }
             if (outs) {
                 download_state(J.C, I, &outs[i], st, stage);
@@ -1263,6 +1433,11 @@ int block_max_cells() { return ::block_max_cells(); }
 int block_threads_for(int maxCells) { return ::block_threads_for(maxCells); }
 void make_slab(btm_case *C, Slab &S) { ::make_slab(C, S); }
 void ensure_mixed(btm_case *C, Slab &S) { ::ensure_mixed(C, S); }
+void ensure_obs(btm_case *C, Slab &S, bool want) { ::ensure_obs(C, S, want); }
+void download_obs(btm_case *C, const btm::DevInst &I, btm_history *h, cudaStream_t st) {
+    ::download_obs(C, I, h, st);
+}
+void free_slab(Slab &S) { ::free_slab(S); }
 void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
                   std::vector<double> &stage) {
     ::upload_state(C, I, ws, st, stage);

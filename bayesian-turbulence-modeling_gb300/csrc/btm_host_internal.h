@@ -18,6 +18,8 @@ struct Slab {
     size_t bytes = 0;
     void *dptr32 = nullptr;   // FP32 bulk of the mixed-precision engine (allocated on first use)
     size_t bytes32 = 0;
+    double *dObs = nullptr;   // observation outputs (allocated on first use)
+    int obsCap = 0;
     btm::DevInst inst{};      // host copy with device pointers
 };
 
@@ -34,6 +36,7 @@ struct btm_case {
     int amgCoarseN = 0;
     int64_t amgValTotal = 0, amgVecTotal = 0;
     std::vector<Slab> slabs;
+    void *obsArena = nullptr;        // observation plan (dmesh.obs points into it)
     std::mutex mtx;
     cudaStream_t stream = nullptr;
 };
@@ -49,6 +52,12 @@ int block_threads_for(int maxCells);
 // instance slab (FP64 fields and work) and its FP32 bulk for the mixed engine
 void make_slab(btm_case *C, Slab &S);
 void ensure_mixed(btm_case *C, Slab &S);
+// observation outputs of an instance: allocated and wired into S.inst when
+// `want` and the case has observables, else S.inst.obsOut = null
+void ensure_obs(btm_case *C, Slab &S, bool want);
+// copies the n_obs predictions and the log-likelihood of a finished instance
+void download_obs(btm_case *C, const btm::DevInst &I, btm_history *h, cudaStream_t st);
+void free_slab(Slab &S);
 // FP64 state between a caller's btm_state and a slab (synchronises `st`)
 void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
                   std::vector<double> &stage);

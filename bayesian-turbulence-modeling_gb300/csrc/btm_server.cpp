@@ -187,6 +187,7 @@ void complete(btm_server *S, Slot &s) {
         for (int q = 0; q < 8; ++q) h->phase_ms[q] = 1e-6 * (double)tns[q];
         h->solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
         h->finish_ms = h->solve_ms;
+        btm_host::download_obs(s.C, I, h, st);
     }
     if (s.req.out) {
         btm_host::download_state(s.C, I, s.req.out, st, S->stage);
@@ -248,10 +249,7 @@ void btm_server_destroy(btm_server *S) {
     if (!S) return;
     for (auto &st : S->streams) if (st) cudaStreamSynchronize(st);
     if (S->copyStream) cudaStreamSynchronize(S->copyStream);
-    for (auto &p : S->slots) {
-        if (p->slab.dptr) cudaFree(p->slab.dptr);
-        if (p->slab.dptr32) cudaFree(p->slab.dptr32);
-    }
+    for (auto &p : S->slots) btm_host::free_slab(p->slab);
     for (auto &kv : S->tags) {
         if (kv.second.d) cudaFree(kv.second.d);
         if (kv.second.ready) cudaEventDestroy(kv.second.ready);
@@ -279,9 +277,8 @@ int btm_server_submit(btm_server *S, const btm_request *r) {
                 // recycle a free slot of another case when the slot count is exhausted
                 for (auto &p : S->slots)
                     if (p->state == Slot::FREE) {
-                        if (p->slab.dptr) cudaFree(p->slab.dptr);
-                        if (p->slab.dptr32) cudaFree(p->slab.dptr32);
                         S->used -= slab_bytes(*p);
+                        btm_host::free_slab(p->slab);
                         const int flag = p->flag;
                         p.reset(new Slot());
                         p->flag = flag;
@@ -300,16 +297,12 @@ int btm_server_submit(btm_server *S, const btm_request *r) {
                 btm_host::make_slab(C, slot->slab);
                 if (mixed) btm_host::ensure_mixed(C, slot->slab);
             } catch (const std::exception &) {
-                if (slot->slab.dptr) cudaFree(slot->slab.dptr);
-                if (slot->slab.dptr32) cudaFree(slot->slab.dptr32);
-                slot->slab = Slab();
+                btm_host::free_slab(slot->slab);
                 slot->C = nullptr;
                 return BTM_EAGAIN;
             }
             if (S->used + slab_bytes(*slot) > S->budget) {
-                cudaFree(slot->slab.dptr);
-                if (slot->slab.dptr32) cudaFree(slot->slab.dptr32);
-                slot->slab = Slab();
+                btm_host::free_slab(slot->slab);
                 slot->C = nullptr;
                 return BTM_EAGAIN;
             }
@@ -341,6 +334,7 @@ int btm_server_submit(btm_server *S, const btm_request *r) {
         }
         I.hist = nullptr;
         I.histCap = 0;
+        btm_host::ensure_obs(C, slot->slab, r->hist && r->hist->predictions);
         S->hFlags[slot->flag] = 0;
         I.doneFlag = S->dFlags + slot->flag;
         sck(cudaMemsetAsync(I.barrier, 0, 512, S->copyStream), "memset control");

@@ -25,7 +25,8 @@ INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 LIB_NAME = "libbtm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["btm_engine.cu", "btm_mixed.cu", "btm_host.cpp", "btm_server.cpp", "btm_noalloc.cu"]
-HEADERS = ["btm_common.h", "btm_host_internal.h", "btm_team.cuh", "btm_bc.cuh", "btm_phases64.cuh"]
+HEADERS = ["btm_common.h", "btm_host_internal.h", "btm_team.cuh", "btm_bc.cuh", "btm_phases64.cuh",
+           "btm_observe.cuh"]
 
 
 def nvcc() -> str:
@@ -47,6 +48,7 @@ def _stamp() -> str:
     with open(os.path.join(INCLUDE, "btm_gb300.h"), "rb") as fh:
         h.update(fh.read())
     h.update(" ".join(ARCH).encode())
+    h.update(b"host-fp-contract-off")
     return h.hexdigest()
 
 
@@ -62,13 +64,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 return out
     cc = nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
+    # host code: no floating-point contraction (gcc on Arm fuses a*b+c into an
+    # FMA by default), so host-side geometry and observation constants round
+    # like the reference and numpy
+    host = ["-Xcompiler", "-ffp-contract=off"]
     jobs = [
         [cc] + common + ["-fmad=false", "-c", os.path.join(CSRC, "btm_engine.cu"), "-o",
                          os.path.join(BUILD, "btm_engine.o")],
-        [cc] + common + ["-x", "cu", "-c", os.path.join(CSRC, "btm_host.cpp"), "-o",
-                         os.path.join(BUILD, "btm_host.o")],
-        [cc] + common + ["-x", "cu", "-c", os.path.join(CSRC, "btm_server.cpp"), "-o",
-                         os.path.join(BUILD, "btm_server.o")],
+        [cc] + common + host + ["-x", "cu", "-c", os.path.join(CSRC, "btm_host.cpp"), "-o",
+                                os.path.join(BUILD, "btm_host.o")],
+        [cc] + common + host + ["-x", "cu", "-c", os.path.join(CSRC, "btm_server.cpp"), "-o",
+                                os.path.join(BUILD, "btm_server.o")],
         [cc] + common + ["-c", os.path.join(CSRC, "btm_noalloc.cu"), "-o", os.path.join(BUILD, "btm_noalloc.o")],
         [cc] + common + ["-c", os.path.join(CSRC, "btm_mixed.cu"), "-o", os.path.join(BUILD, "btm_mixed.o")],
     ]

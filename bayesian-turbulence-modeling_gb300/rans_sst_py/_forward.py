@@ -35,8 +35,12 @@ STATUS_FROM_CODE = {0: EvaluationStatus.Converged, 1: EvaluationStatus.Unconverg
 class SolveOutput:
     """State and convergence record of one device solve."""
 
-    def __init__(self, state: Optional[dict], hist: BtmHistory, residuals=None):
+    def __init__(self, state: Optional[dict], hist: BtmHistory, residuals=None, predictions=None):
         self.state = state
+        # observables of the case's observation operator, evaluated on the
+        # device (None when the case has none attached)
+        self.predictions = [float(v) for v in predictions] if predictions is not None else None
+        self.log_lik = float(hist.log_lik) if predictions is not None else None
         self.status = STATUS_FROM_CODE.get(hist.status, EvaluationStatus.Unknown)
         self.converged = bool(hist.converged)
         self.diverged = bool(hist.diverged)
@@ -72,11 +76,14 @@ def _init_struct(init, keep):
 
 
 def solve_batch(cases: Sequence[Case], coeffs, variants=None, inits=None, want_state=True,
-                history_capacity: int = 0) -> List[SolveOutput]:
+                history_capacity: int = 0, observe: bool = True) -> List[SolveOutput]:
     """Run len(cases) independent solves in one device launch.
 
     coeffs: (n, 11) SST constants; inits: per instance a dict with either
     {"u", "p", "k", "omega"} (cold uniform start) or a full state dict (warm).
+    observe: evaluate the observation operator attached to a case
+    (Case.set_observations) on the device; with want_state=False only the
+    predictions and the log-likelihood leave the device.
     """
     n = len(cases)
     coeffs = np.ascontiguousarray(np.asarray(coeffs, np.float64).reshape(n, 11))
@@ -97,6 +104,12 @@ def solve_batch(cases: Sequence[Case], coeffs, variants=None, inits=None, want_s
             res_bufs[i] = np.zeros((history_capacity, 6))
             hist[i].residual_capacity = history_capacity
             hist[i].residuals = dptr(res_bufs[i])
+    preds = [None] * n
+    if observe:
+        for i in range(n):
+            if cases[i].n_obs > 0:
+                preds[i] = np.zeros(cases[i].n_obs)
+                hist[i].predictions = dptr(preds[i])
     handles = (C.c_void_p * n)(*[c.h.value for c in cases])
     check(lib().btm_solve_batch(n, handles, dptr(coeffs), var.ctypes.data_as(C.POINTER(C.c_int32)),
                                 ini_arr, st_arr if want_state else None, hist))
@@ -107,12 +120,13 @@ def solve_batch(cases: Sequence[Case], coeffs, variants=None, inits=None, want_s
         r = None
         if res_bufs[i] is not None:
             r = res_bufs[i][:min(history_capacity, hist[i].iterations_run)]
-        outs.append(SolveOutput(states[i], hist[i], r))
+        outs.append(SolveOutput(states[i], hist[i], r, preds[i]))
     return outs
 
 
-def solve(case: Case, coeffs, variant: int = 0, init=None, want_state=True, history_capacity=0) -> SolveOutput:
-    return solve_batch([case], [coeffs], [variant], [init], want_state, history_capacity)[0]
+def solve(case: Case, coeffs, variant: int = 0, init=None, want_state=True, history_capacity=0,
+          observe: bool = True) -> SolveOutput:
+    return solve_batch([case], [coeffs], [variant], [init], want_state, history_capacity, observe)[0]
 
 
 class _WarmStartCache:
@@ -183,6 +197,8 @@ class ForwardModel:
     def _get_case(self) -> Case:
         if self._case is None:
             self._case = Case(self._mesh, self._bcs, self._nu, self._settings)
+            if self._obs.n_obs() > 0:
+                self._case.set_observations(self._obs)
         return self._case
 
     def evaluate(self, theta) -> EvaluationResult:
@@ -204,8 +220,12 @@ class ForwardModel:
             if out.converged:
                 self._cache.store(theta, out.state)
             self._last = out.state
-            pred = self._obs.evaluate(self._mesh, out.state, self._nu)
-            ll = self._obs.log_likelihood(self._mesh, out.state, self._nu, pred)
+            # observables and log-likelihood come from the device evaluation
+            # at the end of the solve (ObservationOperator.hpp:186-378)
+            if out.predictions is not None:
+                pred, ll = out.predictions, out.log_lik
+            else:
+                pred, ll = [], 0.0
             return EvaluationResult(status, ll, pred, out.final_iter)
         except Exception as e:  # nothing escapes evaluate (ForwardModel.cpp:99-104)
             if self._settings.verbose:

@@ -65,7 +65,14 @@ class BtmHistory(C.Structure):
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
                 ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8),
                 ("solve_ms", C.c_double), ("finish_ms", C.c_double), ("inner_split", C.c_int64 * 4),
-                ("polish_start", C.c_int32)]
+                ("polish_start", C.c_int32), ("predictions", _dp), ("log_lik", C.c_double)]
+
+
+class BtmObservable(C.Structure):
+    _fields_ = [("type", C.c_int32), ("patch", C.c_int32), ("component", C.c_int32),
+                ("location", C.c_double * 3), ("observed", C.c_double), ("sigma_obs", C.c_double),
+                ("sigma_model", C.c_double), ("ref_area", C.c_double), ("ref_velocity", C.c_double),
+                ("ref_pressure", C.c_double), ("ref_density", C.c_double)]
 
 
 SOLVER_CODES = {"PCG": 0, "BiCGSTAB": 1, "GaussSeidel": 2, "AMG": 3}
@@ -96,6 +103,8 @@ def lib():
             L.btm_case_destroy.restype = None
             L.btm_case_info.argtypes = [C.c_void_p] + [C.POINTER(C.c_int32)] * 4
             L.btm_case_set_settings.argtypes = [C.c_void_p, C.POINTER(BtmSettings)]
+            L.btm_case_set_observations.argtypes = [C.c_void_p, C.POINTER(BtmMesh), C.c_int32,
+                                                    C.POINTER(BtmObservable)]
             L.btm_solve.argtypes = [C.c_void_p, _dp, C.c_int32, C.POINTER(BtmInit), C.POINTER(BtmState),
                                     C.POINTER(BtmHistory)]
             L.btm_solve_noalloc.argtypes = [C.c_void_p, _dp, C.c_int32, C.POINTER(BtmInit), C.POINTER(BtmState),
@@ -246,9 +255,11 @@ class Case:
         h = C.c_void_p()
         check(L.btm_case_create(C.byref(ms), bc, float(nu), C.byref(st), C.byref(h)))
         self.h = h
+        self._mesh = mesh
         self.n_cells = mesh.n_cells()
         self.n_bnd = mesh.n_boundary_faces()
         self.n_internal = mesh.n_internal_faces()
+        self.n_obs = 0
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:
@@ -270,3 +281,23 @@ class Case:
     def set_settings(self, settings):
         st = settings_struct(settings)
         check(self._L.btm_case_set_settings(self.h, C.byref(st)))
+
+    def set_observations(self, obs_op):
+        """Attach an ObservationOperator (None: detach): every later solve of
+        this case evaluates its observables and the log-likelihood on the
+        device (btm_case_set_observations)."""
+        items = obs_op.observables() if obs_op is not None else []
+        arr = (BtmObservable * max(len(items), 1))()
+        mesh = self._mesh
+        for i, o in enumerate(items):
+            a = arr[i]
+            a.type = int(o.type)
+            a.patch = mesh.patch_by_name(o.patchName) if o.patchName else -1
+            a.component = int(o.component)
+            a.location[0], a.location[1], a.location[2] = o.location.x, o.location.y, o.location.z
+            a.observed, a.sigma_obs, a.sigma_model = o.observed, o.sigma_obs, o.sigma_model
+            a.ref_area, a.ref_velocity = o.referenceArea, o.refVelocity
+            a.ref_pressure, a.ref_density = o.refPressure, o.refDensity
+        ms, keep = mesh_struct(mesh)
+        check(self._L.btm_case_set_observations(self.h, C.byref(ms), len(items), arr))
+        self.n_obs = len(items)

@@ -4,10 +4,11 @@ incompressible/src/ParameterSensitivity.cpp:26-37, 691-745).
 
 The reference runs the 22 warm re-solves of eta_jacobian_warm_fd one after
 another; here they are independent instances of one solve_batch launch, each
-warm-started from the same converged state.  Closure fields of a state are
-recomputed on the device (the SST phase, reference-rounded), the nu_t floor
-0.1 nu is applied as the reference does, and the observation operator and the
-Gaussian log-likelihood are evaluated on the result.  The tangent / adjoint
+warm-started from the same converged state, and the observation operator and
+the Gaussian log-likelihood of each are evaluated on the device at the end of
+its solve (only those numbers leave the device).  For observe/log_lik at the
+kept state, closure fields are recomputed on the device (the SST phase,
+reference-rounded) and the nu_t floor 0.1 nu is applied as the reference does.  The tangent / adjoint
 ground-work methods of the reference class are outside the rebuilt path.
 """
 from __future__ import annotations
@@ -117,6 +118,7 @@ class ParameterSensitivity:
         if warm_tol > 0.0:
             warm.convergence_tol = float(warm_tol)
         wcase = Case(self._mesh, self._bcs, self._nu, warm)
+        wcase.set_observations(self._obs)
         steps, thetas = [], []
         for j in range(11):
             hr = min(h_rel, 1e-5) if j in (8, 9) else h_rel
@@ -126,8 +128,10 @@ class ParameterSensitivity:
                 tp = theta.copy()
                 tp[j] += sgn * h
                 thetas.append(tp)
+        # observables and log-likelihoods are evaluated on the device: only
+        # they leave it, not the 22 states
         outs = solve_batch([wcase] * 22, np.array(thetas), [self._settings.sst_variant] * 22,
-                           [self._state] * 22, want_state=True)
+                           [self._state] * 22, want_state=False)
         for o in outs:
             out.n_residual_evals += o.final_iter
         for j in range(11):
@@ -136,8 +140,8 @@ class ParameterSensitivity:
             out.krylov_converged[j] = 1 if ok else 0
             if not ok:
                 continue
-            ep, lp = self._observed(thetas[2 * j], op.state)
-            em, lm = self._observed(thetas[2 * j + 1], om.state)
+            ep, lp = op.predictions, op.log_lik
+            em, lm = om.predictions, om.log_lik
             for i in range(self.n_obs()):
                 out.d_obs_d_theta[i][j] = (ep[i] - em[i]) / (2.0 * steps[j])
             out.log_lik_gradient[j] = (lp - lm) / (2.0 * steps[j])

@@ -10,7 +10,10 @@ A request is admitted when its case has a free solve slot, or a new slot fits
 the slot count and the HBM budget; admitted requests start at the next poll
 or flush while earlier ones keep running, and each finishes on its own.
 `tag` keeps the final state on the device and starts the next request with
-the same tag (and case) from it, as an MCMC chain's last field.
+the same tag (and case) from it, as an MCMC chain's last field.  When the case
+has an observation operator attached (Case.set_observations), each result
+carries the device-evaluated predictions and log-likelihood; with
+want_state=False nothing else leaves the device.
 """
 from __future__ import annotations
 
@@ -74,6 +77,11 @@ class Server:
         state = new_state(case.n_cells, case.n_bnd) if want_state else None
         st = state_struct(state) if want_state else None
         hist = BtmHistory()
+        pred = None
+        if case.n_obs > 0:
+            # observables evaluated on the device at the end of the solve
+            pred = np.zeros(case.n_obs)
+            hist.predictions = dptr(pred)
         req = BtmRequest(rid, case.h.value, dptr(cf), int(variant), C.pointer(ini), int(tag),
                          C.pointer(st) if st is not None else None, C.pointer(hist),
                          BTM_REQ_TAG_NORMS if tag_norms else 0)
@@ -81,7 +89,7 @@ class Server:
         if rc == BTM_EAGAIN:
             return None
         check(rc)
-        self._live[rid] = (case, cf, ini, keep, state, st, hist, req)
+        self._live[rid] = (case, cf, ini, keep, state, st, hist, req, pred)
         return rid
 
     def flush(self):
@@ -97,10 +105,10 @@ class Server:
         done = []
         for i in range(n.value):
             rid = int(ids[i])
-            case, cf, ini, keep, state, st, hist, req = self._live.pop(rid)
+            case, cf, ini, keep, state, st, hist, req, pred = self._live.pop(rid)
             if state is not None:
                 state["turb_established"] = int(st.turb_established)
-            done.append((rid, SolveOutput(state, hist)))
+            done.append((rid, SolveOutput(state, hist, None, pred)))
         return done
 
     def stats(self) -> dict:

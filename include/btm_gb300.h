@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BTM_ABI_VERSION 2
+#define BTM_ABI_VERSION 3
 
 /* ---- status codes -------------------------------------------------------- */
 #define BTM_OK              0
@@ -203,6 +203,13 @@ typedef struct btm_history {
     /* mixed precision: first outer iteration of the FP64-assembly polishing
      * stage (-1: FP64 engine, or the stage never started) */
     int32_t polish_start;
+    /* observables of the case's observation operator (btm_case_set_observations),
+     * evaluated on the device at the end of the solve: `predictions` is the
+     * caller's [n_obs] buffer or NULL (then nothing is evaluated); log_lik is
+     * the Gaussian log-likelihood of those predictions.  Only these n_obs + 1
+     * numbers leave the device when `out` is NULL. */
+    double *predictions;
+    double  log_lik;
 } btm_history;
 
 typedef struct btm_case btm_case;
@@ -222,6 +229,34 @@ int btm_case_info(const btm_case *c, int32_t *n_cells, int32_t *n_boundary_faces
                   int32_t *n_amg_levels, int32_t *is_2d);
 /* Replace the case's SIMPLE controls (same checks as at creation). */
 int btm_case_set_settings(btm_case *c, const btm_settings *settings);
+
+/* ---- observation operator on the device -----------------------------------
+ * The reference ObservationOperator (core/include/ObservationOperator.hpp:46-378)
+ * attached to a case: every solve of the case whose btm_history has a
+ * `predictions` buffer evaluates the observables on the device from the final
+ * state (same nearest-cell / nearest-wall-face choices, first minimum wins;
+ * the same molecular wall-shear formulas and sub-face interpolated zero
+ * crossings; the same operation order, so results are bit-identical to a host
+ * evaluation of the downloaded fields) and the Gaussian log-likelihood
+ * sum_i -0.5 (pred_i - obs_i)^2 / max(sigma_obs^2 + sigma_model^2, 1e-30). */
+#define BTM_OBS_DRAG            0   /* C_D = F_x / (q_ref A_ref) over a wall patch  */
+#define BTM_OBS_PRESSURE_TAP    1   /* C_p at the nearest cell                       */
+#define BTM_OBS_VELOCITY        2   /* U[component] at the nearest cell              */
+#define BTM_OBS_SKIN_FRICTION   3   /* C_f at the nearest face of a wall patch       */
+#define BTM_OBS_SEPARATION      4   /* first +/- zero crossing of tau_x along a patch */
+#define BTM_OBS_REATTACHMENT    5   /* first -/+ zero crossing of tau_x along a patch */
+typedef struct btm_observable {
+    int32_t type;              /* BTM_OBS_*                                       */
+    int32_t patch;             /* patch index (drag, skin friction, crossings)    */
+    int32_t component;         /* velocity component 0, 1, 2                      */
+    double  location[3];       /* probe / tap / skin-friction location            */
+    double  observed, sigma_obs, sigma_model;
+    double  ref_area, ref_velocity, ref_pressure, ref_density;
+} btm_observable;
+/* `mesh` is the mesh the case was created from (the searches run on the host
+ * here, once).  n = 0 removes the operator.  Not while solves of the case are
+ * in flight. */
+int btm_case_set_observations(btm_case *c, const btm_mesh *mesh, int32_t n, const btm_observable *obs);
 
 /* One forward solve on the device.  coeffs[11] are the SST constants in the
  * InferenceParameterSet order (core/include/InferenceParameters.hpp:11-14);

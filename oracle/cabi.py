@@ -60,7 +60,7 @@ class History(C.Structure):
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
                 ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8),
                 ("solve_ms", C.c_double), ("finish_ms", C.c_double), ("inner_split", C.c_int64 * 4),
-                ("polish_start", C.c_int32)]
+                ("polish_start", C.c_int32), ("predictions", C.POINTER(C.c_double)), ("log_lik", C.c_double)]
 
 
 CELL_FIELDS = ("p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw")

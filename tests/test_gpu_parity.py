@@ -313,6 +313,9 @@ def test_forward_model_api():
     r = fm.evaluate(theta)
     assert r.status == rs.EvaluationStatus.Converged
     assert len(r.predictions) == 2 and np.isfinite(r.log_lik)
+    # device-evaluated observables: bit-identical to the host operator
+    host = obs.evaluate(m, fm.last_state(), nu)
+    assert r.predictions == host and r.log_lik == obs.log_likelihood(m, fm.last_state(), nu, host)
     f = fm.last_fields()
     assert set(f) == {"U", "p", "k", "omega", "nuT", "F1", "F2", "Pk"} and f["U"].shape == (m.n_cells(), 3)
     # kappa below its 0.35 bound: InvalidParameters without a solve
