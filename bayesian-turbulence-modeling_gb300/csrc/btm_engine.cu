@@ -194,24 +194,31 @@ __device__ void amg_prolong(T &tm, const DevMesh &M, DevInst &I, int l) {
     tm.sync();
 }
 
+// grid-size dense coarsest inverse (up to kCoarseDirectGrid rows): one warp
+// per row, lane-strided partial sums folded by a butterfly
+template <class T>
+__device__ __noinline__ void amg_coarse_dense_warp(T &tm, const DevMesh &M, DevInst &I) {
+    const int l = M.nLevels - 1;
+    const int n = M.lev[l].n;
+    const double *b = lev_b(I, M, l);
+    double *x = lev_x(I, M, l);
+    const int lane = tm.rank() & 31;
+    for (int i = tm.rank() >> 5; i < n; i += tm.size() >> 5) {
+        const double *row = I.ainv + (size_t)i * n;
+        double s = 0.0;
+        for (int j = lane; j < n; j += 32) s = fma(LD(row + j), LD(b + j), s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) x[i] = s;
+    }
+    tm.sync();
+}
+
 template <class T>
 __device__ void amg_coarse_solve(T &tm, const DevMesh &M, DevInst &I) {
     const int l = M.nLevels - 1;
     const int n = M.lev[l].n;
     if (M.coarseDirect && n > kCoarseDirect) {
-        // grid-size dense inverse: one warp per row, lane-strided partial
-        // sums folded by a butterfly
-        const double *b = lev_b(I, M, l);
-        double *x = lev_x(I, M, l);
-        const int lane = tm.rank() & 31;
-        for (int i = tm.rank() >> 5; i < n; i += tm.size() >> 5) {
-            const double *row = I.ainv + (size_t)i * n;
-            double s = 0.0;
-            for (int j = lane; j < n; j += 32) s = fma(LD(row + j), LD(b + j), s);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) x[i] = s;
-        }
-        tm.sync();
+        amg_coarse_dense_warp(tm, M, I);
     } else if (M.coarseDirect) {
         const double *b = lev_b(I, M, l);
         double *x = lev_x(I, M, l);

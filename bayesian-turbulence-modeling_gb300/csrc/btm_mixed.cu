@@ -788,24 +788,31 @@ __device__ void mx_amg_prolong(T &tm, const DevMesh &M, DevWork32 &F, int l) {
     tm.sync();
 }
 
+// grid-size dense coarsest inverse (up to kCoarseDirectGrid rows): one warp
+// per row, lane-strided partial sums folded by a butterfly
+template <class T>
+__device__ __noinline__ void mx_amg_coarse_dense_warp(T &tm, const DevMesh &M, DevWork32 &F) {
+    const int l = M.nLevels - 1;
+    const int n = M.lev[l].n;
+    const float *b = lev_bf(F, M, l);
+    float *x = lev_xf(F, M, l);
+    const int lane = tm.rank() & 31;
+    for (int i = tm.rank() >> 5; i < n; i += tm.size() >> 5) {
+        const double *row = F.ainv + (size_t)i * n;
+        double s = 0.0;
+        for (int j = lane; j < n; j += 32) s = fma(LD(row + j), (double)LD(b + j), s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) x[i] = (float)s;
+    }
+    tm.sync();
+}
+
 template <class T>
 __device__ void mx_amg_coarse_solve(T &tm, const DevMesh &M, DevWork32 &F) {
     const int l = M.nLevels - 1;
     const int n = M.lev[l].n;
     if (M.coarseDirect && n > kCoarseDirect) {
-        // grid-size dense inverse: one warp per row, lane-strided partial
-        // sums folded by a butterfly
-        const float *b = lev_bf(F, M, l);
-        float *x = lev_xf(F, M, l);
-        const int lane = tm.rank() & 31;
-        for (int i = tm.rank() >> 5; i < n; i += tm.size() >> 5) {
-            const double *row = F.ainv + (size_t)i * n;
-            double s = 0.0;
-            for (int j = lane; j < n; j += 32) s = fma(LD(row + j), (double)LD(b + j), s);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) x[i] = (float)s;
-        }
-        tm.sync();
+        mx_amg_coarse_dense_warp(tm, M, F);
     } else if (M.coarseDirect) {
         const float *b = lev_bf(F, M, l);
         float *x = lev_xf(F, M, l);

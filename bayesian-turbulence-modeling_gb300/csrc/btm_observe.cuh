@@ -54,7 +54,7 @@ __device__ double obs_crossing(const ObsDev &O, const DevInst &I, double nu, int
 
 // predictions into I.obsOut[0, n), the log-likelihood into I.obsOut[n]
 template <class T>
-__device__ void observe_leader(const DevMesh &M, DevInst &I) {
+__device__ __noinline__ void observe_leader(const DevMesh &M, DevInst &I) {
     const ObsDev &O = M.obs;
     const double nu = I.nu;
     double ll = 0.0;

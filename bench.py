@@ -453,6 +453,14 @@ def run_served(args):
     s2.precision = "mixed"
     case_defs = [(rs.Case(m1, b1, nu1, s1), i1, "channel_re180_4x32"), (rs.Case(m2, b2, nu2, s2), i2,
                                                                         "couette_re500_4x32")]
+    # each chain needs its likelihood: skin friction and two velocity probes,
+    # evaluated on the device, are all that leaves it per request
+    for cd, (m, wall) in zip(case_defs, ((m1, "bottom_wall"), (m2, "bottom_wall"))):
+        op = rs.ObservationOperator()
+        op.add_skin_friction(wall, rs.Vec3(0.5, 0.0, 0.5), 0.006, 0.001, 16.0)
+        op.add_velocity_profile(rs.Vec3(0.5, 1.0, 0.5), 0, 18.0, 1.0)
+        op.add_velocity_profile(rs.Vec3(0.5, 0.1, 0.5), 0, 9.0, 1.0)
+        cd[0].set_observations(op)
     rng = np.random.default_rng(SERVED_SEED)
     rate = args.served_rate
     gaps = rng.exponential(1.0 / rate, int(rate * SERVED_SECONDS * 1.5) + 16)
@@ -474,7 +482,7 @@ def run_served(args):
         srv.submit(cdef[0], np.array(tc.COEFF_DEFAULTS), init=cdef[1])
     while srv.pending:
         srv.poll(timeout_ms=20)
-    backlog, arrival_of, latency, iters, conv, service = [], {}, [], [], 0, []
+    backlog, arrival_of, latency, iters, conv, service, lls = [], {}, [], [], 0, [], []
     t0 = time.perf_counter()
     k = 0
     max_inflight = 0
@@ -497,6 +505,7 @@ def run_served(args):
             iters.append(out.iterations_run)
             service.append(out.solve_ms)
             conv += int(out.converged)
+            lls.append(out.log_lik)
         max_inflight = max(max_inflight, srv.stats()["inflight"])
     wall = time.perf_counter() - t0
     st = srv.stats()
@@ -509,6 +518,9 @@ def run_served(args):
                        "cases": [cd[2] for cd in case_defs], "tol": TOL, "precision": "mixed",
                        "warm_start": "device-resident tag per chain; residuals scaled by the chain's "
                                      "cold solve (BTM_REQ_TAG_NORMS)", "max_iterations": SERVED_MAX_ITER},
+            "observables": {"per_request": 3, "log_lik_finite": int(np.isfinite(lls).sum()),
+                            "note": "Cf + 2 velocity probes and the log-likelihood evaluated on the device; "
+                                    "no field leaves the device"},
             "requests": int(len(times)), "invalid_parameters": invalid, "solved": len(latency),
             "converged": conv, "wall_s": wall, "mean_outer_iters": float(np.mean(iters)) if iters else None,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -518,6 +530,57 @@ def run_served(args):
                            "note": "device time of each solve inside the server"},
             "server": {"slots": st["slots"], "bytes": st["bytes"], "max_inflight_seen": max_inflight}}
     print(json.dumps(line), flush=True)
+
+
+def run_large(args):
+    """One large mesh on the cooperative grid (a secondary measurement; the
+    headline is the batch): the permuted 122,880-cell backward-facing step
+    (Re_h 36000, reference BFS settings, FP64 drop-in by default) or the
+    permuted 2.05M-cell periodic square duct (20x320x320, Re_tau 600, mixed
+    precision by default), a fixed number of outer iterations from the cold
+    start.  Reports ms per outer iteration and cell-iterations/s from the
+    launch's CUDA-event time."""
+    import rans_sst_py as rs
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases as tc
+    if args.large == "bfs120k":
+        m = rs.Mesh.make_backward_facing_step_2d(64, 384, 192, 96, 4.0, 30.0, 1.0, 3.0, 36000.0, 1.0)
+        m = m.permuted(np.random.default_rng(7).permutation(m.n_cells()))
+        nu = 1.0 / 36000.0
+        k_in = 1.5 * 0.01 ** 2
+        om_in = k_in / (100.0 * nu)
+        bcs_fn = lambda mm: rs.FlowBoundaryConditions.bfs_defaults(mm, 1.0, k_in, om_in)  # noqa: E731
+        s = tc.bfs_settings(args.large_iters, 0.0)
+        init = dict(u=(1.0, 0.0, 0.0), p=0.0, k=k_in, omega=om_in)
+        prec = args.large_precision or "fp64"
+    else:
+        ratio = tc.ratio_for_first_cell(1.0 / 600.0, 160)
+        m = rs.Mesh.make_square_duct_periodic_3d(20, 320, 320, 10.0, 2.0, ratio)
+        m = m.permuted(np.random.default_rng(17).permutation(m.n_cells()))
+        nu = 1.0 / 600.0
+        bcs_fn = lambda mm: rs.FlowBoundaryConditions.channel_defaults(mm, 0.0, 0.0, 0.0)  # noqa: E731
+        s = tc.channel_settings(args.large_iters, 0.0)
+        init = dict(u=(15.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
+        prec = args.large_precision or "mixed"
+    m.compute_wall_distance(device=True)
+    s.precision = prec
+    case = rs.Case(m, bcs_fn(m), nu, s)
+    out = rs.solve(case, tc.COEFF_DEFAULTS, 0, init, want_state=False)
+    ms = lib_launch_ms()
+    n_it = max(out.iterations_run, 1)
+    line = {"metric": "cell-iterations/s", "value": m.n_cells() * n_it / (ms * 1e-3), "unit": "cell-it/s",
+            "higher_is_better": True, "n_gpus": 1, "dtype": "f64" if prec == "fp64" else "f32+f64",
+            "data": "synthetic", "impl": "gb300",
+            "config": {"workload": args.large, "cells": m.n_cells(), "outer_iterations": n_it, "precision": prec,
+                       "start": "cold", "team": "cooperative grid"},
+            "ms_per_outer_iteration": ms / n_it, "inner_split_per_outer": [v / n_it for v in out.inner_split],
+            "launch_ms": ms}
+    print(json.dumps(line), flush=True)
+
+
+def lib_launch_ms():
+    from rans_sst_py._lib import lib
+    return float(lib().btm_last_launch_ms())
 
 
 def main():
@@ -540,6 +603,11 @@ def main():
     ap.add_argument("--served-rate", type=float, default=SERVED_RATE, help="served stream: arrivals per second")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the plain-FP64 launch of the same batch and the error report")
+    ap.add_argument("--large", choices=["bfs120k", "duct2m"], default=None,
+                    help="one large mesh on the cooperative grid instead of the batch")
+    ap.add_argument("--large-iters", type=int, default=20, help="--large: outer iterations from the cold start")
+    ap.add_argument("--large-precision", choices=["fp64", "mixed"], default=None,
+                    help="--large: engine (default fp64 for bfs120k, mixed for duct2m)")
     args = ap.parse_args()
     global PRECISION
     PRECISION = args.precision
@@ -550,6 +618,10 @@ def main():
     if args.served:
         if rank == 0:
             run_served(args)
+        return
+    if args.large:
+        if rank == 0:
+            run_large(args)
         return
     if args.impl == "reference":
         run_reference(args, world, rank)
