@@ -149,7 +149,7 @@ BYTES_PER_CELL_OUTER_MIXED = 760.0
 BYTES_PER_CELL_INNER_MIXED = 204.0
 # ncu DRAM bytes (read + write) per cell-iteration of the profile case (304
 # instances x 200 outer iterations of the 4x128 channel), per engine.
-TRAFFIC_PER_CELL_ITER = {"fp64": 460.0, "mixed": 55.0}
+TRAFFIC_PER_CELL_ITER = {"fp64": 460.0, "mixed": 58.0}
 FIXED_POINT_SUBSET = 8
 FIXED_POINT_ITERS = 40000
 
