@@ -230,6 +230,26 @@ def dist_max(world, x):
     return x
 
 
+def dist_sum(world, x):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+    return x
+
+
+def aggregate_ranks(world, dev_ms, wall_s, conv_counts):
+    """Whole-job figures over the ranks: the slowest rank's mean step time
+    (device and end-to-end), the converged solves of all ranks per step, and
+    the job throughput = all ranks' converged solves / the slowest step."""
+    step_s = dist_max(world, statistics.mean(dev_ms) / 1e3)
+    e2e_s = dist_max(world, statistics.mean(wall_s))
+    converged = dist_sum(world, statistics.mean(conv_counts))
+    return step_s, e2e_s, converged, converged / step_s, converged / e2e_s
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -316,11 +336,8 @@ def run_gpu(args, world, rank, local):
             inner += sum(o.inner_iterations for o in outs)
     dist_barrier(world)
     clk = clocks.summary()
-    step_s = dist_max(world, statistics.mean(dev_ms) / 1e3)
+    step_s, e2e_s, converged_all, value, e2e_value = aggregate_ranks(world, dev_ms, wall_s, conv_counts)
     converged = statistics.mean(conv_counts)
-    value = world * converged / step_s
-    e2e_s = dist_max(world, statistics.mean(wall_s))
-    e2e_value = world * converged / e2e_s
     h2d = n * (11 * 8 + 4 + 48)
     nb = m.n_boundary_faces()
     d2h = n * 8 * (m.n_cells() * 11 + nb * 6)

@@ -1,0 +1,57 @@
+"""The N>1 path of bench.py on CPU: two gloo ranks (one process per GPU in a
+real run) share no data-path collective; only the timing aggregation crosses
+ranks.  Whole-job throughput is all ranks' converged solves over the slowest
+rank's step, and the reference arm runs on rank 0 alone."""
+import os
+import socket
+import sys
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.multiprocessing as mp  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    import bench
+    w, r, local = bench.dist_setup()
+    assert (w, r, local) == (world, rank, rank)
+    bench.dist_barrier(w)
+    # rank 1 is the slower one; each rank converged a different count per step
+    dev_ms = [[100.0, 110.0], [150.0, 170.0]][rank]
+    wall_s = [[0.2, 0.2], [0.3, 0.5]][rank]
+    conv = [[219, 219], [218, 220]][rank]
+    step_s, e2e_s, converged, value, e2e_value = bench.aggregate_ranks(w, dev_ms, wall_s, conv)
+    # the reference arm: ranks other than 0 exit without work
+    ran_reference = bench.run_reference(None, w, r) if r != 0 else None
+    out[rank] = (step_s, e2e_s, converged, value, e2e_value, ran_reference)
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+@pytest.mark.timeout(300)
+def test_two_gloo_ranks_aggregate_max_and_sum():
+    world = 2
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_rank_main, args=(world, _free_port(), out), nprocs=world, join=True)
+    assert set(out.keys()) == {0, 1}
+    for rank in (0, 1):
+        step_s, e2e_s, converged, value, e2e_value, ran_ref = out[rank]
+        assert step_s == pytest.approx(0.160)          # max of the ranks' mean device steps
+        assert e2e_s == pytest.approx(0.4)            # max of the mean end-to-end steps
+        assert converged == pytest.approx(438.0)      # 219 + 219 converged solves per step
+        assert value == pytest.approx(438.0 / 0.160)
+        assert e2e_value == pytest.approx(438.0 / 0.4)
+    assert out[1][5] is None
