@@ -108,6 +108,9 @@ struct DevMesh {
     int64_t amgValTotal, amgVecTotal;
     DevGeom32 g32;
     ObsDev obs;
+    // Reynolds-stress injection target anisotropy [6*nC] (xx yy zz xy xz yz
+    // per cell), null when injection is off
+    const double *bTarget;
 };
 
 // Scalar controls of one solve (SolverSettings fields read by the loop).
@@ -117,6 +120,7 @@ struct DevSettings {
     double convTol, divLimit, alphaU, alphaP, alphaK, alphaW, innerTol;
     double bodyForce[3];
     double kMin, kMax, omegaMin, vonKarman;
+    double alphaInj;       // blend factor of the Reynolds-stress injection source
 };
 
 // FP32 bulk of one mixed-precision instance: closure fields, gradients, the
@@ -188,6 +192,9 @@ struct DevInst {
     // observation outputs [obs.n + 1]: predictions, then the log-likelihood
     // (null: not evaluated)
     double *obsOut;
+    // Reynolds-stress injection: the blended source [3][nC] (x, y, z) and the
+    // deferred-correction tensor D [6][nC]; null when the case has no target
+    double *inj;
     // served requests: completion flag in mapped host memory (null otherwise),
     // set by the leader after every output is written
     volatile int32_t *doneFlag;

@@ -509,6 +509,7 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
                 phase_velgrad(tm, M, I, 1 << (comp - 1));
                 tm.sync();
             }
+            if (comp == 0 && I.inj) phase_inj(tm, M, I, I.g, I.nut, iter == 0);
             phase_mom_faces(tm, M, I, comp);
             tm.sync();
             phase_mom_cells(tm, M, I, comp);

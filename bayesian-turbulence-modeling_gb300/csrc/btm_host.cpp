@@ -328,6 +328,7 @@ btm::DevSettings dev_settings(const btm_settings &s) {
     d.kMax = s.k_max;
     d.omegaMin = s.omega_min;
     d.vonKarman = s.von_karman;
+    d.alphaInj = s.alpha_injection;
     return d;
 }
 
@@ -812,12 +813,51 @@ void free_slab(Slab &S) {
     if (S.dptr) cudaFree(S.dptr);
     if (S.dptr32) cudaFree(S.dptr32);
     if (S.dObs) cudaFree(S.dObs);
+    if (S.dInj) cudaFree(S.dInj);
     S = Slab();
+}
+
+void ensure_inj(btm_case *C, Slab &S) {
+    if (!C->dmesh.bTarget) {
+        S.inst.inj = nullptr;
+        return;
+    }
+    if (!S.dInj) ck(cudaMalloc((void **)&S.dInj, sizeof(double) * 9 * (size_t)C->nC), "cudaMalloc(injection)");
+    S.inst.inj = S.dInj;
+}
+
+// aniso::sym3Eigenvalues + barycentricMargin (core/include/AnisotropyTools.hpp:23-67):
+// descending eigenvalues of the symmetric target by the trigonometric closed
+// form, then the most negative barycentric coordinate
+double barycentric_margin(const double *b) {
+    const double xx = b[0], yy = b[1], zz = b[2], xy = b[3], xz = b[4], yz = b[5];
+    const double q = (xx + yy + zz) / 3.0;
+    const double dxx = xx - q, dyy = yy - q, dzz = zz - q;
+    const double p2 = (dxx * dxx + dyy * dyy + dzz * dzz + 2.0 * (xy * xy + xz * xz + yz * yz)) / 6.0;
+    const double p = std::sqrt(std::max(p2, 0.0));
+    double l0, l1, l2;
+    if (p < 1e-30) {
+        l0 = l1 = l2 = q;
+    } else {
+        const double inv = 1.0 / p;
+        const double m00 = dxx * inv, m11 = dyy * inv, m22 = dzz * inv;
+        const double m01 = xy * inv, m02 = xz * inv, m12 = yz * inv;
+        double r = 0.5 * (m00 * (m11 * m22 - m12 * m12) - m01 * (m01 * m22 - m12 * m02) +
+                          m02 * (m01 * m12 - m11 * m02));
+        r = std::max(-1.0, std::min(1.0, r));
+        const double phi = std::acos(r) / 3.0;
+        l0 = q + 2.0 * p * std::cos(phi);
+        l2 = q + 2.0 * p * std::cos(phi + 2.0943951023931953);
+        l1 = 3.0 * q - l0 - l2;
+    }
+    const double c1 = l0 - l1, c2 = 2.0 * (l1 - l2), c3 = 3.0 * l2 + 1.0;
+    return std::min(c1, std::min(c2, c3));
 }
 
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
     I.S = dev_settings(C->settings);
     I.obsOut = nullptr;
+    I.inj = nullptr;
     I.nu = C->nu;
     for (int q = 0; q < 11; ++q) I.coeff[q] = coeffs[q];
     I.variant = variant;
@@ -951,6 +991,7 @@ void btm_case_destroy(btm_case *C) {
     for (Slab &s : C->slabs) free_slab(s);
     if (C->meshArena) cudaFree(C->meshArena);
     if (C->obsArena) cudaFree(C->obsArena);
+    if (C->injTarget) cudaFree(C->injTarget);
     if (C->dMeshPtr) cudaFree(C->dMeshPtr);
     if (C->stream) cudaStreamDestroy(C->stream);
     delete C;
@@ -980,6 +1021,62 @@ int btm_case_set_settings(btm_case *C, const btm_settings *s) {
         if (e != cudaSuccess) return fail(BTM_ERR_CUDA, cudaGetErrorString(e));
     }
     C->settings = *s;
+    return BTM_OK;
+}
+
+// ForwardModel::setTargetAnisotropy (incompressible/src/ForwardModel.cpp:22-26)
+// for the case: the target on the device and its realizability, checked once
+// (SIMPLESolver.cpp:295-307 re-checks the same constant target every outer
+// iteration).
+int btm_case_set_target_anisotropy(btm_case *C, const double *b6) {
+    if (!C) return fail(BTM_ERR_ARG, "null case");
+    try {
+        double *dT = nullptr;
+        bool allReal = true;
+        double maxViol = 0.0;
+        if (b6) {
+            for (size_t i = 0; i < 6 * (size_t)C->nC; ++i)
+                if (!std::isfinite(b6[i])) throw BtmError(BTM_ERR_ARG, "target anisotropy has a non-finite entry");
+            for (int c = 0; c < C->nC; ++c) {
+                const double margin = barycentric_margin(b6 + 6 * (size_t)c);
+                if (margin < -1e-6) {
+                    allReal = false;
+                    maxViol = std::max(maxViol, -margin);
+                }
+            }
+            ck(cudaMalloc((void **)&dT, sizeof(double) * 6 * (size_t)C->nC), "cudaMalloc(target anisotropy)");
+            cudaError_t e = cudaMemcpy(dT, b6, sizeof(double) * 6 * (size_t)C->nC, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                cudaFree(dT);
+                throw BtmError(BTM_ERR_CUDA, cudaGetErrorString(e));
+            }
+        }
+        btm::DevMesh D = C->dmesh;
+        D.bTarget = dT;
+        cudaError_t e = cudaMemcpy(C->dMeshPtr, &D, sizeof D, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            if (dT) cudaFree(dT);
+            throw BtmError(BTM_ERR_CUDA, cudaGetErrorString(e));
+        }
+        if (C->injTarget) cudaFree(C->injTarget);
+        C->injTarget = dT;
+        C->dmesh = D;
+        C->injAllRealizable = allReal;
+        C->injMaxViolation = maxViol;
+    } catch (const BtmError &e) {
+        return fail(e.code, e.what());
+    } catch (const std::exception &e) {
+        return fail(BTM_ERR_INTERNAL, e.what());
+    }
+    return BTM_OK;
+}
+
+int btm_case_injection_realizability(const btm_case *C, int32_t *active, int32_t *all_realizable,
+                                     double *max_violation) {
+    if (!C) return fail(BTM_ERR_ARG, "null case");
+    if (active) *active = C->dmesh.bTarget ? 1 : 0;
+    if (all_realizable) *all_realizable = C->injAllRealizable ? 1 : 0;
+    if (max_violation) *max_violation = C->injMaxViolation;
     return BTM_OK;
 }
 
@@ -1107,6 +1204,7 @@ int btm_case_set_observations(btm_case *C, const btm_mesh *m, int32_t n, const b
             throw BtmError(BTM_ERR_CUDA, cudaGetErrorString(e));
         }
         if (C->obsArena) cudaFree(C->obsArena);
+    if (C->injTarget) cudaFree(C->injTarget);
         C->obsArena = arena;
         C->dmesh = D;
     } catch (const BtmError &e) {
@@ -1171,6 +1269,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             const bool mixed = J.C->settings.precision == BTM_PREC_MIXED;
             if (mixed) ensure_mixed(J.C, *J.S);
             ensure_obs(J.C, *J.S, hists && hists[i].predictions);
+            ensure_inj(J.C, *J.S);
             if (mixed && J.C->nC <= block_max_cells()) {
                 mixIdx.push_back(i);
             } else if (!mixed && J.C->nC <= block_max_cells()) {
@@ -1438,6 +1537,7 @@ void download_obs(btm_case *C, const btm::DevInst &I, btm_history *h, cudaStream
     ::download_obs(C, I, h, st);
 }
 void free_slab(Slab &S) { ::free_slab(S); }
+void ensure_inj(btm_case *C, Slab &S) { ::ensure_inj(C, S); }
 void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
                   std::vector<double> &stage) {
     ::upload_state(C, I, ws, st, stage);

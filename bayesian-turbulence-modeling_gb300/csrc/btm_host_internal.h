@@ -20,6 +20,7 @@ struct Slab {
     size_t bytes32 = 0;
     double *dObs = nullptr;   // observation outputs (allocated on first use)
     int obsCap = 0;
+    double *dInj = nullptr;   // injection blend and tensor [9*nC] (allocated on first use)
     btm::DevInst inst{};      // host copy with device pointers
 };
 
@@ -37,6 +38,9 @@ struct btm_case {
     int64_t amgValTotal = 0, amgVecTotal = 0;
     std::vector<Slab> slabs;
     void *obsArena = nullptr;        // observation plan (dmesh.obs points into it)
+    double *injTarget = nullptr;     // injection target anisotropy (dmesh.bTarget)
+    bool injAllRealizable = true;
+    double injMaxViolation = 0.0;
     std::mutex mtx;
     cudaStream_t stream = nullptr;
 };
@@ -58,6 +62,9 @@ void ensure_obs(btm_case *C, Slab &S, bool want);
 // copies the n_obs predictions and the log-likelihood of a finished instance
 void download_obs(btm_case *C, const btm::DevInst &I, btm_history *h, cudaStream_t st);
 void free_slab(Slab &S);
+// injection work of an instance: allocated and wired into S.inst when the
+// case has a target anisotropy, else S.inst.inj = null
+void ensure_inj(btm_case *C, Slab &S);
 // FP64 state between a caller's btm_state and a slab (synchronises `st`)
 void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
                   std::vector<double> &stage);

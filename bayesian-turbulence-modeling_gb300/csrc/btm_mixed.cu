@@ -359,7 +359,8 @@ __device__ __noinline__ double mx_mom_cells(T &tm, const DevMesh &M, DevInst &I,
         const float vol = G.vol[c];
         float src = ts - gp[c] * vol;
         if (fb != 0.0f) src = fmaf(fb, vol, src);
-        const double rc = (double)src - flux;
+        double rc = (double)src - flux;
+        if (I.inj) rc += LD(I.inj + (size_t)comp * M.nC + c);   // injection source, FP64
         rr = fma(rc, rc, rr);
         F.src[c] = (float)rc;
         const float dr = diag / alphaU;
@@ -1182,6 +1183,13 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
             if (comp == 2 && !I.solveZ) break;
             double *u = comp == 0 ? I.ux : (comp == 1 ? I.uy : I.uz);
             double rr[1];
+            if (comp == 0 && I.inj) {
+                // the injection force from this iteration's gradients and
+                // eddy viscosity (FP64 in the polishing stage, the FP32
+                // copies in stage 1)
+                if (polish) phase_inj(tm, M, I, I.g, I.nut, iter == 0);
+                else phase_inj(tm, M, I, F.g, F.nut, iter == 0);
+            }
             if (polish) {
                 if (comp > 0) {
                     phase_velgrad<T, true>(tm, M, I, 1 << (comp - 1));

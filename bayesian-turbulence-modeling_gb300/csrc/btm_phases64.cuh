@@ -277,6 +277,84 @@ __device__ __noinline__ void phase_mom_faces(T &tm, const DevMesh &M, DevInst &I
     }
 }
 
+// Reynolds-stress injection source (SIMPLESolver::addInjectionSource,
+// incompressible/src/SIMPLESolver.cpp:224-315), run before the x-momentum
+// assembly of every outer iteration.  Per cell the deferred-correction tensor
+// D = 2 k b_target + 2 nu_t dev(S) from the velocity gradients `g`
+// (g[3*i+j] = dU_i/dx_j) and eddy viscosity `nut` (FP64, or the mixed
+// engine's FP32 stage-1 copies); per cell the
+// force q = -sum_f (D_f . n_f) A_f gathered over its internal faces in
+// ascending face order (D_f distance-weighted, owner side subtracts) and then
+// its boundary faces (owner value), the reference's scatter order; then
+// blend = q on the first pass of a solve (or alpha >= 1), else
+// blend (1 - alpha) + q alpha.  inj[0..3nC) holds the blend, inj[3nC..9nC) D.
+template <class T, class G>
+__device__ __noinline__ void phase_inj(T &tm, const DevMesh &M, DevInst &I, const G *const *g, const G *nut,
+                                       bool first) {
+    const int nC = M.nC;
+    double *D = I.inj + 3 * (size_t)nC;
+    // the mixed engine's stage 1 skips the w gradients of a 2-D instance
+    // (identically zero there)
+    const bool wGrad = sizeof(G) == 8 || I.solveZ != 0;
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const double g6 = wGrad ? (double)LD(g[6] + c) : 0.0, g7 = wGrad ? (double)LD(g[7] + c) : 0.0;
+        const double S11 = LD(g[0] + c), S22 = LD(g[4] + c), S33 = wGrad ? (double)LD(g[8] + c) : 0.0;
+        const double S12 = 0.5 * ((double)LD(g[1] + c) + (double)LD(g[3] + c));
+        const double S13 = 0.5 * ((double)LD(g[2] + c) + g6);
+        const double S23 = 0.5 * ((double)LD(g[5] + c) + g7);
+        const double trS3 = (S11 + S22 + S33) / 3.0;
+        const double twoK = 2.0 * LD(I.k + c), twoNu = 2.0 * (double)LD(nut + c);
+        const double *bt = M.bTarget + 6 * (size_t)c;
+        D[0 * (size_t)nC + c] = twoK * bt[0] + twoNu * (S11 - trS3);
+        D[1 * (size_t)nC + c] = twoK * bt[1] + twoNu * (S22 - trS3);
+        D[2 * (size_t)nC + c] = twoK * bt[2] + twoNu * (S33 - trS3);
+        D[3 * (size_t)nC + c] = twoK * bt[3] + twoNu * S12;
+        D[4 * (size_t)nC + c] = twoK * bt[4] + twoNu * S13;
+        D[5 * (size_t)nC + c] = twoK * bt[5] + twoNu * S23;
+    }
+    tm.sync();
+    const double r = I.S.alphaInj;
+    const bool fresh = first || r >= 1.0;
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        double qx = 0.0, qy = 0.0, qz = 0.0;
+        for (int e = M.cfOff[c]; e < M.cfOff[c + 1]; ++e) {
+            const int f = M.cfFace[e], oth = M.cfOther[e];
+            const int o = oth >= 0 ? c : -(oth + 1), n = oth >= 0 ? oth : c;
+            const double w = M.w[f], wn = 1.0 - w;
+            double d[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) d[k] = w * LD(D + k * (size_t)nC + o) + wn * LD(D + k * (size_t)nC + n);
+            const double nx = M.nx[f], ny = M.ny[f], nz = M.nz[f], A = M.area[f];
+            const double fx = (d[0] * nx + d[3] * ny + d[4] * nz) * A;
+            const double fy = (d[3] * nx + d[1] * ny + d[5] * nz) * A;
+            const double fz = (d[4] * nx + d[5] * ny + d[2] * nz) * A;
+            if (oth >= 0) { qx = qx - fx; qy = qy - fy; qz = qz - fz; }
+            else { qx = qx + fx; qy = qy + fy; qz = qz + fz; }
+        }
+        for (int e = M.cbOff[c]; e < M.cbOff[c + 1]; ++e) {
+            const int b = M.cbFace[e];
+            double d[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) d[k] = LD(D + k * (size_t)nC + c);
+            const double nx = M.bnx[b], ny = M.bny[b], nz = M.bnz[b], A = M.barea[b];
+            qx = qx - (d[0] * nx + d[3] * ny + d[4] * nz) * A;
+            qy = qy - (d[3] * nx + d[1] * ny + d[5] * nz) * A;
+            qz = qz - (d[4] * nx + d[5] * ny + d[2] * nz) * A;
+        }
+        double *bl = I.inj;
+        if (fresh) {
+            bl[c] = qx;
+            bl[nC + c] = qy;
+            bl[2 * (size_t)nC + c] = qz;
+        } else {
+            bl[c] = LD(bl + c) * (1.0 - r) + qx * r;
+            bl[nC + c] = LD(bl + nC + c) * (1.0 - r) + qy * r;
+            bl[2 * (size_t)nC + c] = LD(bl + 2 * (size_t)nC + c) * (1.0 - r) + qz * r;
+        }
+    }
+    tm.sync();
+}
+
 // Cell pass of the momentum system (diag, source, relaxation).
 template <class T, bool Fast = false>
 __device__ __noinline__ void phase_mom_cells(T &tm, const DevMesh &M, DevInst &I, int comp) {
@@ -330,6 +408,7 @@ __device__ __noinline__ void phase_mom_cells(T &tm, const DevMesh &M, DevInst &I
         src = src - LD(gp + c) * vol;
         if (fb != 0.0) src = src + fb * vol;
         src = src + ts;
+        if (I.inj) src = src + LD(I.inj + (size_t)comp * M.nC + c);
         const double phi_old = LD(Uc + c);
         if (Fast) {
             src = src + relaxSrc * diag * phi_old;

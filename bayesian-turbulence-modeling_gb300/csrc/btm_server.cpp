@@ -335,6 +335,7 @@ int btm_server_submit(btm_server *S, const btm_request *r) {
         I.hist = nullptr;
         I.histCap = 0;
         btm_host::ensure_obs(C, slot->slab, r->hist && r->hist->predictions);
+        btm_host::ensure_inj(C, slot->slab);
         S->hFlags[slot->flag] = 0;
         I.doneFlag = S->dFlags + slot->flag;
         sck(cudaMemsetAsync(I.barrier, 0, 512, S->copyStream), "memset control");

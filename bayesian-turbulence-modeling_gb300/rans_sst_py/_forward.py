@@ -173,6 +173,9 @@ class _WarmStartCache:
             self._q.clear()
 
 
+_NO_INJECTION = {"active": False, "checked_iters": 0, "all_realizable": True, "max_violation": 0.0}
+
+
 class ForwardModel:
     """Drop-in for rans_sst_py.ForwardModel (python/Bindings.cpp:468-519)."""
 
@@ -193,12 +196,16 @@ class ForwardModel:
         self._cache = _WarmStartCache(50, 0.5)
         self._last: Optional[dict] = None
         self._last_solve: Optional[SolveOutput] = None
+        self._b6: Optional[np.ndarray] = None
+        self._last_inj = _NO_INJECTION.copy()
 
     def _get_case(self) -> Case:
         if self._case is None:
             self._case = Case(self._mesh, self._bcs, self._nu, self._settings)
             if self._obs.n_obs() > 0:
                 self._case.set_observations(self._obs)
+            if self._b6 is not None:
+                self._case.set_target_anisotropy(self._b6)
         return self._case
 
     def evaluate(self, theta) -> EvaluationResult:
@@ -208,16 +215,25 @@ class ForwardModel:
         try:
             coeffs = self._param_set.unpack(theta).to_vector()
             case = self._get_case()
-            warm = self._cache.find_nearest(theta)
+            # injected solves neither read nor fill the warm-start cache
+            # (ForwardModel.cpp:50-57, 83-85)
+            injected = self._b6 is not None
+            warm = None if injected else self._cache.find_nearest(theta)
             out = solve(case, coeffs, int(self._settings.sst_variant), warm if warm is not None else self._init)
             self._last_solve = out
+            if injected:
+                _, real, viol = case.injection_realizability()
+                self._last_inj = {"active": True, "checked_iters": out.iterations_run, "all_realizable": real,
+                                  "max_violation": viol}
+            else:
+                self._last_inj = _NO_INJECTION.copy()
             if out.status == EvaluationStatus.Unknown:
                 raise RuntimeError("device solve abandoned")
             if out.diverged:
                 self._last = None
                 return EvaluationResult(EvaluationStatus.DivergenceDetected, -1e6, [], out.final_iter)
             status = EvaluationStatus.Converged if out.converged else EvaluationStatus.Unconverged
-            if out.converged:
+            if out.converged and not injected:
                 self._cache.store(theta, out.state)
             self._last = out.state
             # observables and log-likelihood come from the device evaluation
@@ -263,15 +279,32 @@ class ForwardModel:
     def clear_cache(self) -> None:
         self._cache.clear()
 
-    # Reynolds-stress injection is outside the rebuilt hot path.
+    # ---- a-posteriori Reynolds-stress injection (python/Bindings.cpp:485-518,
+    # ForwardModel.hpp:110-118): the per-cell target is applied on the device
+    # by every later evaluate() until cleared
     def set_target_anisotropy(self, b_target):
-        raise NotImplementedError("Reynolds-stress injection is not part of the GB300 forward model")
+        b = np.asarray(b_target, np.float64)
+        if b.ndim != 3 or b.shape[1] != 3 or b.shape[2] != 3:
+            raise RuntimeError("set_target_anisotropy: expected (n_cells, 3, 3)")
+        b6 = np.empty((b.shape[0], 6))
+        b6[:, 0], b6[:, 1], b6[:, 2] = b[:, 0, 0], b[:, 1, 1], b[:, 2, 2]
+        b6[:, 3] = 0.5 * (b[:, 0, 1] + b[:, 1, 0])
+        b6[:, 4] = 0.5 * (b[:, 0, 2] + b[:, 2, 0])
+        b6[:, 5] = 0.5 * (b[:, 1, 2] + b[:, 2, 1])
+        if b6.size != 6 * self._mesh.n_cells():
+            raise RuntimeError("setTargetAnisotropy: expected nCells*6 values")
+        self._b6 = b6.reshape(-1)
+        if self._case is not None:
+            self._case.set_target_anisotropy(self._b6)
 
     def clear_target_anisotropy(self):
-        return None
+        self._b6 = None
+        if self._case is not None:
+            self._case.set_target_anisotropy(None)
 
     def has_target_anisotropy(self) -> bool:
-        return False
+        return self._b6 is not None
 
     def injection_diagnostics(self):
-        return {"active": False, "checked_iters": 0, "all_realizable": True, "max_violation": 0.0}
+        """InjectionDiagnostics of the last evaluate (SIMPLESolver.hpp:83-88)."""
+        return dict(self._last_inj)

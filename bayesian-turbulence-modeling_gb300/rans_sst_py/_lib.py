@@ -46,7 +46,7 @@ class BtmSettings(C.Structure):
                 ("omega_min", C.c_double), ("use_wall_functions", C.c_int32),
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
-                ("turbulence_solver", C.c_int32), ("precision", C.c_int32)]
+                ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double)]
 
 
 class BtmState(C.Structure):
@@ -105,6 +105,9 @@ def lib():
             L.btm_case_set_settings.argtypes = [C.c_void_p, C.POINTER(BtmSettings)]
             L.btm_case_set_observations.argtypes = [C.c_void_p, C.POINTER(BtmMesh), C.c_int32,
                                                     C.POINTER(BtmObservable)]
+            L.btm_case_set_target_anisotropy.argtypes = [C.c_void_p, _dp]
+            L.btm_case_injection_realizability.argtypes = [C.c_void_p, C.POINTER(C.c_int32),
+                                                           C.POINTER(C.c_int32), C.POINTER(C.c_double)]
             L.btm_solve.argtypes = [C.c_void_p, _dp, C.c_int32, C.POINTER(BtmInit), C.POINTER(BtmState),
                                     C.POINTER(BtmHistory)]
             L.btm_solve_noalloc.argtypes = [C.c_void_p, _dp, C.c_int32, C.POINTER(BtmInit), C.POINTER(BtmState),
@@ -216,6 +219,7 @@ def settings_struct(s) -> BtmSettings:
     if prec not in PRECISION_CODES:
         raise ValueError(f"precision must be one of {sorted(PRECISION_CODES)}, not {prec!r}")
     st.precision = PRECISION_CODES[prec]
+    st.alpha_injection = float(getattr(s, "alpha_injection", 0.3))
     return st
 
 
@@ -301,3 +305,21 @@ class Case:
         ms, keep = mesh_struct(mesh)
         check(self._L.btm_case_set_observations(self.h, C.byref(ms), len(items), arr))
         self.n_obs = len(items)
+
+    def set_target_anisotropy(self, b6):
+        """Reynolds-stress injection target, (n_cells*6,) xx yy zz xy xz yz
+        per cell, applied to every later solve of the case; None clears it
+        (btm_case_set_target_anisotropy)."""
+        if b6 is None:
+            check(self._L.btm_case_set_target_anisotropy(self.h, None))
+            return
+        b6 = np.ascontiguousarray(np.asarray(b6, np.float64).reshape(-1))
+        if b6.size != 6 * self.n_cells:
+            raise RuntimeError("setTargetAnisotropy: expected nCells*6 values")
+        check(self._L.btm_case_set_target_anisotropy(self.h, dptr(b6)))
+
+    def injection_realizability(self):
+        """(active, all_realizable, max_violation) of the case's target."""
+        a, r, v = C.c_int32(), C.c_int32(), C.c_double()
+        check(self._L.btm_case_injection_realizability(self.h, C.byref(a), C.byref(r), C.byref(v)))
+        return bool(a.value), bool(r.value), float(v.value)

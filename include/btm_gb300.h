@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BTM_ABI_VERSION 3
+#define BTM_ABI_VERSION 4
 
 /* ---- status codes -------------------------------------------------------- */
 #define BTM_OK              0
@@ -151,6 +151,8 @@ typedef struct btm_settings {
     int32_t momentum_solver;
     int32_t turbulence_solver;
     int32_t precision;             /* BTM_PREC_*; not a reference field */
+    double  alpha_injection;       /* blend factor of the Reynolds-stress
+                                      injection source (alphaInjection) */
 } btm_settings;
 
 /* Initial state.  mode 0 = cold uniform start exactly as
@@ -229,6 +231,22 @@ int btm_case_info(const btm_case *c, int32_t *n_cells, int32_t *n_boundary_faces
                   int32_t *n_amg_levels, int32_t *is_2d);
 /* Replace the case's SIMPLE controls (same checks as at creation). */
 int btm_case_set_settings(btm_case *c, const btm_settings *settings);
+
+/* ---- a-posteriori Reynolds-stress injection -------------------------------
+ * ForwardModel::setTargetAnisotropy / clearTargetAnisotropy
+ * (incompressible/src/ForwardModel.cpp:22-26, ForwardModel.hpp:110-118): a
+ * per-cell target anisotropy b6[6*n_cells] (xx yy zz xy xz yz) adds, to every
+ * later solve of the case, the explicit deferred-correction momentum source
+ * -div(2 k b_target + 2 nu_t dev(S)) blended over the outer iterations at
+ * settings.alpha_injection (SIMPLESolver.cpp:205-315).  b6 = NULL clears it.
+ * The realizability check of the target (barycentric margin of its
+ * eigenvalues >= -1e-6, core/include/AnisotropyTools.hpp) runs here once:
+ * the target does not change during a solve. */
+int btm_case_set_target_anisotropy(btm_case *c, const double *b6);
+/* Realizability of the case's target: 1/0 and the worst violation (>= 0);
+ * *active = 0 when no target is set. */
+int btm_case_injection_realizability(const btm_case *c, int32_t *active, int32_t *all_realizable,
+                                     double *max_violation);
 
 /* ---- observation operator on the device -----------------------------------
  * The reference ObservationOperator (core/include/ObservationOperator.hpp:46-378)

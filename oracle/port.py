@@ -41,6 +41,8 @@ def lib():
                                    C.POINTER(Settings), dp, C.c_int, C.POINTER(Init),
                                    C.c_void_p, C.POINTER(History)]
         L.oracle_green_gauss.argtypes = [C.POINTER(MeshDesc), dp, dp, dp]
+        L.oracle_set_target_anisotropy.argtypes = [dp]
+        L.oracle_set_target_anisotropy.restype = None
         L.oracle_sst_fields.argtypes = [C.POINTER(MeshDesc), dp, C.c_int, C.c_double] + [dp] * 12
         L.oracle_assemble.argtypes = [C.POINTER(MeshDesc), C.POINTER(PatchBC), C.c_double,
                                       C.POINTER(Settings), dp, C.c_int, C.c_void_p, dp, dp,
@@ -125,6 +127,7 @@ def settings_struct(s) -> Settings:
     st.pressure_solver = SOLVER_CODES.get(getattr(s, "pressure_solver", "AMG"), 1)
     st.momentum_solver = SOLVER_CODES.get(getattr(s, "momentum_solver", "BiCGSTAB"), 1)
     st.turbulence_solver = SOLVER_CODES.get(getattr(s, "turbulence_solver", "BiCGSTAB"), 1)
+    st.alpha_injection = float(getattr(s, "alpha_injection", 0.3))
     return st
 
 
@@ -145,8 +148,9 @@ def make_init(u=(1.0, 0.0, 0.0), p=0.0, k=1e-4, omega=1.0, warm=None):
 
 # ---- calls -----------------------------------------------------------------
 def solve(mesh, bcs, nu, settings, coeffs, variant=0, u=(1.0, 0.0, 0.0), p=0.0, k=1e-4,
-          omega=1.0, warm=None, residual_capacity=0):
-    """Run the restated SIMPLE solve; returns (state dict, history dict)."""
+          omega=1.0, warm=None, residual_capacity=0, b_target=None):
+    """Run the restated SIMPLE solve; returns (state dict, history dict).
+    b_target: Reynolds-stress injection target, (n_cells*6,) xx yy zz xy xz yz."""
     m = mesh_arrays(mesh)
     md, keep_m = mesh_desc(m)
     bca, keep_b = bc_array(bcs)
@@ -161,8 +165,13 @@ def solve(mesh, bcs, nu, settings, coeffs, variant=0, u=(1.0, 0.0, 0.0), p=0.0, 
         hist.residual_capacity = residual_capacity
         hist.residuals = _d(res)
     cf = np.ascontiguousarray(coeffs, np.float64)
-    lib().oracle_solve(C.byref(md), bca, float(nu), C.byref(st), _d(cf), int(variant), C.byref(ini),
-                       C.cast(C.pointer(state), C.c_void_p), C.byref(hist))
+    bt = None if b_target is None else np.ascontiguousarray(np.asarray(b_target, np.float64).reshape(-1))
+    lib().oracle_set_target_anisotropy(_d(bt) if bt is not None else None)
+    try:
+        lib().oracle_solve(C.byref(md), bca, float(nu), C.byref(st), _d(cf), int(variant), C.byref(ini),
+                           C.cast(C.pointer(state), C.c_void_p), C.byref(hist))
+    finally:
+        lib().oracle_set_target_anisotropy(None)
     arrays["turb_established"] = state.turb_established
     h = dict(status=hist.status, converged=hist.converged, diverged=hist.diverged,
              final_iter=hist.final_iter, iterations_run=hist.iterations_run,

@@ -89,6 +89,7 @@ SolverSettings toSettings(const btm_settings *s, int variant, int verbose) {
     o.pressureSolver = solverName(s->pressure_solver);
     o.momentumSolver = solverName(s->momentum_solver);
     o.turbulenceSolver = solverName(s->turbulence_solver);
+    o.alphaInjection = s->alpha_injection;
     o.sstVariant = variant;
     o.verbose = verbose != 0;
     o.reportInterval = 1000;
@@ -153,7 +154,15 @@ void vecOut(const VectorField &f, double *out, double *bout) {
 
 }  // namespace
 
+// target anisotropy of the following ref_solve calls (empty: none)
+std::vector<double> g_bTarget6;
+
 extern "C" {
+
+void ref_set_target_anisotropy(const double *b6, int n_cells) {
+    if (b6) g_bTarget6.assign(b6, b6 + 6 * (size_t)n_cells);
+    else g_bTarget6.clear();
+}
 
 const char *ref_last_error(void) { return g_err.c_str(); }
 
@@ -291,6 +300,7 @@ int ref_solve(void *mp, const btm_patch_bc *bcs, double nu, const btm_settings *
         FlowBoundaryConditions bc = toBCs(m, bcs);
         SolverSettings s = toSettings(st, variant, verbose);
         SIMPLESolver solver(m, sst, bc, nu, s);
+        if (!g_bTarget6.empty()) solver.setTargetAnisotropy(&g_bTarget6);
         FlowFields f(m);
         if (init->mode == 0) {
             solver.initUniform(f, Vec3(init->u[0], init->u[1], init->u[2]), init->p, init->k,

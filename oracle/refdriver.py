@@ -55,6 +55,8 @@ def lib():
         L.ref_solve.argtypes = [vp, C.POINTER(PatchBC), C.c_double, C.POINTER(Settings), dp, C.c_int,
                                 C.POINTER(Init), C.POINTER(State), C.POINTER(History), C.c_int]
         L.ref_green_gauss.argtypes = [vp, dp, dp, dp]
+        L.ref_set_target_anisotropy.argtypes = [dp, C.c_int]
+        L.ref_set_target_anisotropy.restype = None
         L.ref_sst_fields.argtypes = [vp, dp, C.c_int, C.c_double] + [dp] * 12
         L.ref_linear_solve.argtypes = [C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, dp, dp, C.c_int,
                                        C.c_double, dp]
@@ -155,8 +157,10 @@ class RefMesh:
         return types.reshape(np_, 4), vals.reshape(np_, 6)
 
     def solve(self, bcs, nu: float, settings: Settings, coeffs, variant: int, init: Init,
-              n_cells: int, n_bnd: int, residual_capacity: int = 0, verbose: int = 0):
+              n_cells: int, n_bnd: int, residual_capacity: int = 0, verbose: int = 0, b_target=None):
         arrays, st = state_arrays(n_cells, n_bnd)
+        bt = None if b_target is None else np.ascontiguousarray(np.asarray(b_target, np.float64).reshape(-1))
+        lib().ref_set_target_anisotropy(_d(bt) if bt is not None else None, n_cells)
         hist = History()
         res = None
         if residual_capacity:
@@ -164,8 +168,11 @@ class RefMesh:
             hist.residual_capacity = residual_capacity
             hist.residuals = _d(res)
         cf = np.ascontiguousarray(coeffs, np.float64)
-        rc = lib().ref_solve(self.h, bcs, nu, C.byref(settings), _d(cf), variant, C.byref(init),
-                             C.byref(st), C.byref(hist), verbose)
+        try:
+            rc = lib().ref_solve(self.h, bcs, nu, C.byref(settings), _d(cf), variant, C.byref(init),
+                                 C.byref(st), C.byref(hist), verbose)
+        finally:
+            lib().ref_set_target_anisotropy(None, 0)
         if rc != 0:
             raise RuntimeError(lib().ref_last_error().decode())
         arrays["turb_established"] = st.turb_established

@@ -619,7 +619,16 @@ typedef struct {
     v3 *gradTmp;
     double *tmp, *tmpb;
     int64_t innerIters;
+    /* Reynolds-stress injection (SIMPLESolver.hpp:93-105) */
+    const double *bTarget6;
+    v3 *injBlend;
+    int injHave;
+    double injRelax;
 } Solver;
+
+/* target anisotropy of the next oracle_solve (NULL: no injection) */
+static const double *g_bTarget6 = NULL;
+void oracle_set_target_anisotropy(const double *b6) { g_bTarget6 = b6; }
 
 static void solver_init(Solver *S, const btm_mesh *m, const btm_patch_bc *bcs, double nu,
                         const btm_settings *s, const double *coeffs, int variant) {
@@ -642,6 +651,7 @@ static void solver_init(Solver *S, const btm_mesh *m, const btm_patch_bc *bcs, d
     S->tmpb = xcalloc(S->nB > 0 ? S->nB : 1, 8);
 }
 static void solver_free(Solver *S) {
+    free(S->injBlend);
     free(S->isWall); free(S->aP); free(S->aPunrelaxed);
     free(S->vg.dudx); free(S->vg.dvdx); free(S->vg.dwdx); free(S->gradTmp);
     free(S->tmp); free(S->tmpb);
@@ -819,6 +829,62 @@ static void transpose_stress(Solver *S, const Fields *f, int comp, double *src) 
 #undef GCOL
 }
 
+/* SIMPLESolver::addInjectionSource (SIMPLESolver.cpp:224-315): on the x pass
+ * the deferred-correction tensor D = 2 k b + 2 nuT dev(S) per cell, the force
+ * q = -sum_f (D_f . n_f) A_f (internal faces in face order, then boundary
+ * faces with the owner value) and its blend at injRelax; every pass adds the
+ * blend's component to the source. */
+static v3 ddotn(const double *d, v3 n) {
+    return mk(d[0] * n.x + d[3] * n.y + d[4] * n.z, d[3] * n.x + d[1] * n.y + d[5] * n.z,
+              d[4] * n.x + d[5] * n.y + d[2] * n.z);
+}
+static void add_injection(Solver *S, Lsys *sys, const Fields *f, int comp) {
+    const btm_mesh *m = S->m;
+    int nC = S->nC;
+    if (comp == 0) {
+        velocity_gradients(m, f->U, f->Ub, &S->vg, S->tmp, S->tmpb);
+        double *D = xcalloc(6 * (size_t)nC, 8);
+        for (int ci = 0; ci < nC; ++ci) {
+            const double S11 = S->vg.dudx[ci].x, S22 = S->vg.dvdx[ci].y, S33 = S->vg.dwdx[ci].z;
+            const double S12 = 0.5 * (S->vg.dudx[ci].y + S->vg.dvdx[ci].x);
+            const double S13 = 0.5 * (S->vg.dudx[ci].z + S->vg.dwdx[ci].x);
+            const double S23 = 0.5 * (S->vg.dvdx[ci].z + S->vg.dwdx[ci].y);
+            const double trS3 = (S11 + S22 + S33) / 3.0;
+            const double twoK = 2.0 * f->k[ci], twoNu = 2.0 * f->nuT[ci];
+            const double *bt = S->bTarget6 + 6 * (size_t)ci;
+            D[6 * ci + 0] = twoK * bt[0] + twoNu * (S11 - trS3);
+            D[6 * ci + 1] = twoK * bt[1] + twoNu * (S22 - trS3);
+            D[6 * ci + 2] = twoK * bt[2] + twoNu * (S33 - trS3);
+            D[6 * ci + 3] = twoK * bt[3] + twoNu * S12;
+            D[6 * ci + 4] = twoK * bt[4] + twoNu * S13;
+            D[6 * ci + 5] = twoK * bt[5] + twoNu * S23;
+        }
+        v3 *q = xcalloc(nC, sizeof(v3));
+        for (int fi = 0; fi < S->nIF; ++fi) {
+            int o = m->owner[fi], n = m->neighbour[fi];
+            double w = m->face_weight[fi], Df[6];
+            for (int c = 0; c < 6; ++c) Df[c] = w * D[6 * o + c] + (1.0 - w) * D[6 * n + c];
+            v3 flux = vmul(ddotn(Df, fnormal(m, fi)), m->face_area[fi]);
+            q[o] = vsub(q[o], flux);
+            q[n] = vadd(q[n], flux);
+        }
+        for (int fi = S->nIF; fi < S->nF; ++fi) {
+            int o = m->owner[fi];
+            q[o] = vsub(q[o], vmul(ddotn(D + 6 * o, fnormal(m, fi)), m->face_area[fi]));
+        }
+        if (!S->injHave || S->injRelax >= 1.0) {
+            memcpy(S->injBlend, q, sizeof(v3) * nC);
+        } else {
+            for (int ci = 0; ci < nC; ++ci)
+                S->injBlend[ci] = vadd(vmul(S->injBlend[ci], 1.0 - S->injRelax), vmul(q[ci], S->injRelax));
+        }
+        S->injHave = 1;
+        free(q);
+        free(D);
+    }
+    for (int ci = 0; ci < nC; ++ci) sys->source[ci] += vcomp(S->injBlend[ci], comp);
+}
+
 /* SIMPLESolver::assembleMomentum (SIMPLESolver.cpp:56-203) */
 static void assemble_momentum(Solver *S, Lsys *sys, const Fields *f, int comp, double *aP) {
     const btm_mesh *m = S->m;
@@ -876,6 +942,7 @@ static void assemble_momentum(Solver *S, Lsys *sys, const Fields *f, int comp, d
     transpose_stress(S, f, comp, tsrc);
     for (int ci = 0; ci < S->nC; ++ci) sys->source[ci] += tsrc[ci];
     free(tsrc);
+    if (S->bTarget6) add_injection(S, sys, f, comp);
     double alphaU = st->alpha_u;
     for (int ci = 0; ci < S->nC; ++ci) {
         double phi_old = vcomp(f->U[ci], comp);
@@ -1280,6 +1347,13 @@ int oracle_solve(const btm_mesh *m, const btm_patch_bc *bcs, double nu, const bt
                  btm_history *hist) {
     Solver S;
     solver_init(&S, m, bcs, nu, s, coeffs, variant);
+    if (g_bTarget6) {
+        /* SIMPLESolver::solve clears the blend and takes alphaInjection (:706-709) */
+        S.bTarget6 = g_bTarget6;
+        S.injBlend = xcalloc(S.nC, sizeof(v3));
+        S.injHave = 0;
+        S.injRelax = s->alpha_injection;
+    }
     Fields f;
     fields_alloc(&f, S.nC, S.nB > 0 ? S.nB : 1);
     if (init->mode == 0)

@@ -22,6 +22,11 @@ int oracle_solve(const btm_mesh *m, const btm_patch_bc *bcs, double nu, const bt
                  const double *coeffs, int variant, const btm_init *init, btm_state *out,
                  btm_history *hist);
 
+/* Target anisotropy [6*n_cells] (xx yy zz xy xz yz) for the following
+ * oracle_solve calls (SIMPLESolver::setTargetAnisotropy, SIMPLESolver.hpp:89);
+ * NULL switches the injection source off.  The array must outlive the calls. */
+void oracle_set_target_anisotropy(const double *b6);
+
 /* greenGaussGrad (core/include/Field.hpp:122-152): grad is n_cells*3. */
 void oracle_green_gauss(const btm_mesh *m, const double *phi, const double *phib, double *grad);
 

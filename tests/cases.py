@@ -39,6 +39,18 @@ def ratio_for_first_cell(y1: float, n_half: int, h: float = 1.0) -> float:
     return 0.5 * (lo + hi)
 
 
+def injection_target(m) -> np.ndarray:
+    """A realizable Reynolds-stress injection target for channel meshes,
+    (n_cells*6,) xx yy zz xy xz yz: fixed normal anisotropies and a shear
+    anisotropy 0.15 tanh(3 (y - 1)) that changes sign across the centreline
+    with the mean shear (the sign of the Boussinesq b_xy = -nu_t S_xy / k)."""
+    eta = m.cell_center[:, 1] - 1.0
+    b = np.zeros((m.n_cells(), 6))
+    b[:, 0], b[:, 1], b[:, 2] = 0.12, -0.08, -0.04
+    b[:, 3] = 0.15 * np.tanh(3.0 * eta)
+    return b.reshape(-1)
+
+
 def channel_settings(max_iter: int, tol: float) -> SolverSettings:
     s = SolverSettings()
     s.verbose = False

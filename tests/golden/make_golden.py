@@ -38,7 +38,7 @@ def settings_json(s) -> np.ndarray:
     return np.frombuffer(json.dumps(d, sort_keys=True).encode(), np.uint8)
 
 
-def ref_solve(mesh_bytes, mesh, bcs, nu, s, init, coeffs=COEFF, variant=0, residual_capacity=0):
+def ref_solve(mesh_bytes, mesh, bcs, nu, s, init, coeffs=COEFF, variant=0, residual_capacity=0, b_target=None):
     path = "/tmp/_golden_mesh.msh"
     with open(path, "wb") as fh:
         fh.write(mesh_bytes)
@@ -49,7 +49,7 @@ def ref_solve(mesh_bytes, mesh, bcs, nu, s, init, coeffs=COEFF, variant=0, resid
     ini, _ = port.make_init(**init)
     t0 = time.time()
     arrays, hist, res = rm.solve(bca, nu, st, coeffs, variant, ini, mesh.n_cells(), mesh.n_boundary_faces(),
-                                 residual_capacity)
+                                 residual_capacity, b_target=b_target)
     dt = time.time() - t0
     info = dict(final_iter=hist.final_iter, iterations_run=hist.iterations_run, converged=hist.converged,
                 diverged=hist.diverged, seconds=dt)
@@ -219,8 +219,30 @@ def make_units():
     return out
 
 
+def make_chan180_inject():
+    """Reynolds-stress injection (SIMPLESolver.cpp:205-315) on the Re_tau 180
+    4x32 channel: cases.injection_target (a realizable, wall-normal varying
+    shear anisotropy with the sign of the mean shear) at the default alphaInjection 0.3; 50 iterations from
+    the cold start, the converged stop and the stagnation state."""
+    m, bcs, nu, init = cases.periodic_channel(32, 180.0)
+    b6 = cases.injection_target(m)
+    s = cases.channel_settings(50, 0.0)
+    mb, out = base_record(m, nu, s, init)
+    out["b_target"] = b6
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init, b_target=b6)
+    pack("pin50", a, info, out)
+    s.max_iterations, s.convergence_tol = 20000, 1e-8
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init, b_target=b6)
+    pack("conv", a, info, out)
+    s.max_iterations, s.convergence_tol = 20000, 0.0
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init, b_target=b6)
+    pack("stag", a, info, out)
+    return out
+
+
 MAKERS = {"units": make_units, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
-          "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1}
+          "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1,
+          "chan180_inject_4x32": make_chan180_inject}
 # makers that extend an existing file instead of producing a new case
 EXTENDERS = {"bfs_perm_1920": add_bfs_continuation}
 

@@ -1,0 +1,146 @@
+"""Reynolds-stress injection (SIMPLESolver.cpp:205-315) on the device, against
+the oracle and the reference's own injected solves (tests/golden/
+chan180_inject_4x32.npz: the Re_tau 180 channel with cases.injection_target).
+
+Tolerances: 60 iterations with tightly converged inner solves against the
+oracle, 1e-8 (FP64) / 1e-5 (mixed) relative L2; the FP64 engine run to the
+reference's stagnation count, 1e-8; the mixed engine converged to the 1e-8
+scaled residual, 1e-6 of the reference's stagnated fields."""
+import json
+
+import numpy as np
+import pytest
+
+import cases
+import rans_sst_py as rs
+from rans_sst_py import Case, FlowBoundaryConditions, SolverSettings, Vec3, solve, solve_batch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return cases.load_golden("chan180_inject_4x32")
+
+
+def _inputs(g):
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    m.compute_wall_distance()
+    d = json.loads(bytes(g["settings"]).decode())
+    s = SolverSettings()
+    for k, v in d.items():
+        setattr(s, k, Vec3(*v) if k == "body_force" else v)
+    a = g["init"]
+    init = dict(u=tuple(a[:3]), p=float(a[3]), k=float(a[4]), omega=float(a[5]))
+    return m, FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0), float(g["nu"]), s, init
+
+
+def _case(g, precision, iters, tol, inner_tol=None):
+    m, bcs, nu, s, init = _inputs(g)
+    s.max_iterations, s.convergence_tol, s.precision = iters, tol, precision
+    if inner_tol is not None:
+        s.inner_tolerance = inner_tol
+    c = Case(m, bcs, nu, s)
+    c.set_target_anisotropy(g["b_target"])
+    return m, bcs, nu, s, init, c
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 1e-5)])
+def test_injection_short_vs_oracle(golden, oracle, precision, tol):
+    m, bcs, nu, s, init, c = _case(golden, precision, 60, 0.0, inner_tol=1e-12)
+    out = solve(c, cases.COEFF_DEFAULTS, 0, init)
+    ref, _ = oracle.solve(m, bcs, nu, s, cases.COEFF_DEFAULTS, 0, **init, b_target=golden["b_target"])
+    for f in ("U", "k", "omega", "nuT"):
+        assert _rel(out.state[f], ref[f]) <= tol, f
+    # the source acts: the plain solve of the same 60 iterations differs
+    c.set_target_anisotropy(None)
+    plain = solve(c, cases.COEFF_DEFAULTS, 0, init)
+    assert _rel(plain.state["U"], out.state["U"]) > 1e-4
+
+
+def test_injection_stagnation_parity(golden):
+    """FP64 engine, the reference's stagnation iteration count: 1e-8."""
+    m, bcs, nu, s, init, c = _case(golden, "fp64", int(golden["stag_iterations_run"]), 0.0)
+    out = solve(c, cases.COEFF_DEFAULTS, 0, init)
+    for f in ("U", "k", "omega", "nuT"):
+        assert _rel(out.state[f], golden[f"stag_{f}"]) <= 1e-8, f
+    # p up to its level: on the periodic channel (no pressure boundary) the
+    # level is set by the start-up path only (here both runs end 3.6e-5 apart,
+    # uniformly); its variation matches within 1e-8 of the dynamic pressure
+    dyn = 0.5 * np.max(np.abs(golden["stag_U"])) ** 2
+    dp = (out.state["p"] - out.state["p"].mean()) - (golden["stag_p"] - golden["stag_p"].mean())
+    assert np.max(np.abs(dp)) <= 1e-8 * dyn
+
+
+def test_injection_mixed_converged(golden):
+    """Mixed engine to the 1e-8 scaled residual: within 1e-6 of the
+    reference's stagnated injected fields."""
+    m, bcs, nu, s, init, c = _case(golden, "mixed", 20000, 1e-8)
+    out = solve(c, cases.COEFF_DEFAULTS, 0, init)
+    assert out.converged
+    for f in ("U", "k", "omega", "nuT"):
+        assert _rel(out.state[f], golden[f"stag_{f}"]) <= 1e-6, f
+
+
+def test_injection_batch_matches_solo(golden):
+    """An injected case and a plain case in one launch: each instance gives
+    the bits it gives alone."""
+    m, bcs, nu, s, init, c = _case(golden, "fp64", 300, 0.0)
+    plain = Case(m, bcs, nu, s)
+    th = np.array(cases.COEFF_DEFAULTS)
+    mix = solve_batch([c, plain, c], [th, th, th * 1.01], None, [init] * 3)
+    solo_inj = solve(c, th, 0, init)
+    solo_plain = solve(plain, th, 0, init)
+    for f in ("U", "p", "k", "omega", "nuT"):
+        assert np.array_equal(mix[0].state[f], solo_inj.state[f])
+        assert np.array_equal(mix[1].state[f], solo_plain.state[f])
+    assert not np.array_equal(mix[0].state["U"], mix[1].state["U"])
+
+
+def test_injection_forward_model_api(golden):
+    """set/clear/has_target_anisotropy, injection_diagnostics, the shape
+    check, and injected solves leaving the warm-start cache alone."""
+    m, bcs, nu, s, init = _inputs(golden)
+    s.max_iterations, s.convergence_tol = 20000, 1e-6
+    ps = rs.InferenceParameterSet.from_indices("c3", [8, 0, 1, 9, 2, 10])
+    fm = rs.ForwardModel(m, ps, rs.ObservationOperator(), bcs, nu, s, rs.Vec3(*init["u"]), init["p"], init["k"],
+                         init["omega"])
+    theta = ps.pack(rs.SSTCoefficients())
+    assert not fm.has_target_anisotropy()
+    assert fm.injection_diagnostics() == {"active": False, "checked_iters": 0, "all_realizable": True,
+                                          "max_violation": 0.0}
+    with pytest.raises(RuntimeError):
+        fm.set_target_anisotropy(np.zeros((m.n_cells(), 3, 2)))
+    with pytest.raises(RuntimeError):
+        fm.set_target_anisotropy(np.zeros((m.n_cells() + 1, 3, 3)))
+    b6 = golden["b_target"].reshape(-1, 6)
+    b = np.zeros((m.n_cells(), 3, 3))
+    b[:, 0, 0], b[:, 1, 1], b[:, 2, 2] = b6[:, 0], b6[:, 1], b6[:, 2]
+    b[:, 0, 1] = b[:, 1, 0] = b6[:, 3]
+    fm.set_target_anisotropy(b)
+    assert fm.has_target_anisotropy()
+    r = fm.evaluate(theta)
+    assert r.status == rs.EvaluationStatus.Converged
+    d = fm.injection_diagnostics()
+    assert d["active"] and d["all_realizable"] and d["max_violation"] == 0.0
+    assert d["checked_iters"] == fm._last_solve.iterations_run
+    assert fm.cache_size() == 0
+    inj_U = fm.last_fields()["U"]
+    fm.clear_target_anisotropy()
+    r2 = fm.evaluate(theta)
+    assert r2.status == rs.EvaluationStatus.Converged
+    assert fm.injection_diagnostics()["active"] is False
+    assert fm.cache_size() == 1
+    assert np.abs(fm.last_fields()["U"] - inj_U).max() > 1e-3
+    # an unrealizable target is reported, not projected
+    bad = b.copy()
+    bad[:, 1, 1] = -0.6     # smallest eigenvalue below -1/3: barycentric C3 < 0
+    fm.set_target_anisotropy(bad)
+    active, realizable, violation = fm._case.injection_realizability()
+    lam = np.linalg.eigvalsh(bad)[:, ::-1]          # descending
+    c = np.stack([lam[:, 0] - lam[:, 1], 2.0 * (lam[:, 1] - lam[:, 2]), 3.0 * lam[:, 2] + 1.0], axis=1)
+    assert active and realizable is False and violation == pytest.approx(-c.min(), rel=1e-9)

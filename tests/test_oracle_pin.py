@@ -167,3 +167,27 @@ def test_duct_short_pin(oracle):
         st, h = oracle.solve(m, bcs, float(g["nu"]), s, cases.COEFF_DEFAULTS, 0, **init_from(g))
         for f in FIELDS:
             assert_same(st[f], g[f"pin{n}_{f}"], 0.0 if SAME_PLATFORM else 1e-12)
+
+
+@pytest.mark.parametrize("stage", ["pin50", "conv"])
+def test_injection_pin(oracle, stage):
+    """Reynolds-stress injection (SIMPLESolver.cpp:205-315) on the Re_tau 180
+    channel: 50 iterations from the cold start, and the cold solve to the 1e-8
+    scaled residual (same stopping iteration, same state)."""
+    g = cases.load_golden("chan180_inject_4x32")
+    m = mesh_from(g)
+    s = settings_from(g)
+    if stage == "pin50":
+        s.max_iterations, s.convergence_tol = 50, 0.0
+    else:
+        s.max_iterations, s.convergence_tol = 20000, 1e-8
+    bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    assert np.array_equal(cases.injection_target(m), g["b_target"])
+    st, h = oracle.solve(m, bcs, float(g["nu"]), s, cases.COEFF_DEFAULTS, 0, **init_from(g),
+                         b_target=g["b_target"])
+    if stage == "conv":
+        assert h["converged"] == 1
+        if SAME_PLATFORM:
+            assert h["final_iter"] == int(g["conv_final_iter"])
+    for f in FIELDS:
+        assert_same(st[f], g[f"{stage}_{f}"], 0.0 if SAME_PLATFORM else 1e-9)
