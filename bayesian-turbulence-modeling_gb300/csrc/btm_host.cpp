@@ -345,7 +345,11 @@ void check_settings(const btm_settings &s) {
         throw BtmError(BTM_ERR_ARG, "unknown precision code");
 }
 
-void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
+// hostOnly: stop after the (validated) host AMG hierarchy and return it
+// without touching the device; forceGrid >= 0 overrides whether the mesh is
+// treated as a cooperative-grid mesh (test hook)
+void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs, std::vector<HLevel> *hostOnly = nullptr,
+                int forceGrid = -1) {
     const int nC = m->n_cells, nF = m->n_faces, nIF = m->n_internal_faces, nP = m->n_patches;
     if (nC <= 0 || nF < nIF || nIF < 0 || nP < 0) throw BtmError(BTM_ERR_ARG, "bad mesh sizes");
     const int nB = nF - nIF;
@@ -535,7 +539,8 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
     }
     // cooperative-grid meshes keep a dense coarsest level of up to
     // kCoarseDirectGrid rows (level 0 is always coarsened once)
-    const int directMax = nC > block_max_cells() ? btm::kCoarseDirectGrid : btm::kCoarseDirect;
+    const bool gridMesh = forceGrid >= 0 ? forceGrid != 0 : nC > block_max_cells();
+    const int directMax = gridMesh ? btm::kCoarseDirectGrid : btm::kCoarseDirect;
     while ((int)lv.size() < btm::kMaxLevels && lv.back().n > btm::kCoarseDirect &&
            (lv.size() == 1 || lv.back().n > directMax)) {
         HLevel &F = lv.back();
@@ -588,6 +593,11 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs) {
             if ((int)L.aggOff.size() != lv[l + 1].n + 1 || L.aggOff.back() != L.n)
                 throw BtmError(BTM_ERR_INTERNAL, "aggOff");
         }
+    }
+
+    if (hostOnly) {
+        *hostOnly = std::move(lv);
+        return;
     }
 
     // ---- upload ------------------------------------------------------------
@@ -959,6 +969,48 @@ extern "C" {
 const char *btm_last_error(void) { return g_err.c_str(); }
 double btm_last_launch_ms(void) { return g_launch_ms; }
 int btm_abi_version(void) { return BTM_ABI_VERSION; }
+
+// Test hook: the host AMG hierarchy btm_case_create builds for `mesh` (no
+// device involved).  grid: 1 / 0 treat the mesh as a cooperative-grid mesh or
+// not, -1 decide by size.  Outputs: the level count, each level's size, the
+// aggregation maps of the levels that have one (concatenated, level 0 first)
+// and level 0's CSR (rows sorted by column; values of the geometric pressure
+// Laplacian the aggregation runs on).  Pass NULL arrays to query the sizes:
+// *maps_len and *nnz0 are always set.
+int btm_debug_amg_hierarchy(const btm_mesh *mesh, const btm_patch_bc *bcs, int32_t grid, int32_t *n_levels,
+                            int32_t *sizes, int32_t *maps, int32_t *maps_len, int32_t *row_ptr0, int32_t *col0,
+                            double *val0, int32_t *nnz0) {
+    if (!mesh || !n_levels || !maps_len || !nnz0 || (mesh->n_patches > 0 && !bcs))
+        return fail(BTM_ERR_ARG, "null argument");
+    btm_case *C = new btm_case();
+    try {
+        std::vector<HLevel> lv;
+        build_case(C, mesh, bcs, &lv, grid);
+        *n_levels = (int32_t)lv.size();
+        int32_t len = 0;
+        for (const HLevel &L : lv) len += (int32_t)L.map.size();
+        *maps_len = len;
+        *nnz0 = (int32_t)lv[0].colIdx.size();
+        if (sizes)
+            for (size_t l = 0; l < lv.size(); ++l) sizes[l] = lv[l].n;
+        if (maps) {
+            int32_t at = 0;
+            for (const HLevel &L : lv)
+                for (int v : L.map) maps[at++] = v;
+        }
+        if (row_ptr0) std::copy(lv[0].rowPtr.begin(), lv[0].rowPtr.end(), row_ptr0);
+        if (col0) std::copy(lv[0].colIdx.begin(), lv[0].colIdx.end(), col0);
+        if (val0) std::copy(lv[0].val.begin(), lv[0].val.end(), val0);
+    } catch (const BtmError &e) {
+        delete C;
+        return fail(e.code, e.what());
+    } catch (const std::exception &e) {
+        delete C;
+        return fail(BTM_ERR_INTERNAL, e.what());
+    }
+    delete C;
+    return BTM_OK;
+}
 
 int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu, const btm_settings *settings,
                     btm_case **out) {

@@ -389,6 +389,16 @@ int btm_debug_phase(btm_case *c, int32_t phase, const double *coeffs,
                     int32_t variant, int32_t arg, const double *in, int64_t n_in,
                     double *out, int64_t n_out);
 
+/* Test hook (no device needed): the host AMG hierarchy btm_case_create builds
+ * for `mesh` - the reference's greedy aggregation (LinearSolver.hpp:407-443)
+ * on the geometric pressure Laplacian, with the cooperative-grid rules when
+ * grid = 1 (0: block rules, -1: by size).  Outputs the level count and sizes
+ * [20], the aggregation maps of the levels that have one (concatenated, level
+ * 0 first) and level 0's CSR; NULL arrays query *maps_len and *nnz0 only. */
+int btm_debug_amg_hierarchy(const btm_mesh *mesh, const btm_patch_bc *bcs, int32_t grid, int32_t *n_levels,
+                            int32_t *sizes, int32_t *maps, int32_t *maps_len, int32_t *row_ptr0, int32_t *col0,
+                            double *val0, int32_t *nnz0);
+
 #ifdef __cplusplus
 }
 #endif

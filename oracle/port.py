@@ -43,6 +43,8 @@ def lib():
         L.oracle_green_gauss.argtypes = [C.POINTER(MeshDesc), dp, dp, dp]
         L.oracle_set_target_anisotropy.argtypes = [dp]
         L.oracle_set_target_anisotropy.restype = None
+        L.oracle_amg_levels.argtypes = [C.c_int, ip, ip, dp, C.c_int, ip, ip]
+        L.oracle_amg_levels.restype = C.c_int
         L.oracle_sst_fields.argtypes = [C.POINTER(MeshDesc), dp, C.c_int, C.c_double] + [dp] * 12
         L.oracle_assemble.argtypes = [C.POINTER(MeshDesc), C.POINTER(PatchBC), C.c_double,
                                       C.POINTER(Settings), dp, C.c_int, C.c_void_p, dp, dp,
@@ -239,3 +241,21 @@ def linear_solve(kind, own, nbr, diag, upper, lower, source, x0, max_iter, tol):
     lib().oracle_linear_solve(int(kind), x.size, own.size, _i(own), _i(nbr), *[_d(v) for v in a],
                               _d(x), int(max_iter), float(tol), _d(res))
     return x, res
+
+
+def amg_levels(row_ptr, col_idx, values, max_levels=21):
+    """AMGSolver::setup's coarsening on a CSR matrix: (sizes, [maps per level])."""
+    n = len(row_ptr) - 1
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    ci = np.ascontiguousarray(col_idx, np.int32)
+    va = np.ascontiguousarray(values, np.float64)
+    sizes = np.zeros(max_levels, np.int32)
+    maps = np.zeros(max(1, n * max_levels), np.int32)
+    nl = lib().oracle_amg_levels(n, rp.ctypes.data_as(C.POINTER(C.c_int)), ci.ctypes.data_as(C.POINTER(C.c_int)),
+                                 _d(va), max_levels, sizes.ctypes.data_as(C.POINTER(C.c_int)),
+                                 maps.ctypes.data_as(C.POINTER(C.c_int)))
+    out, at = [], 0
+    for l in range(nl - 1):
+        out.append(maps[at:at + sizes[l]].copy())
+        at += sizes[l]
+    return sizes[:nl].tolist(), out

@@ -522,6 +522,43 @@ static void amg_setup(Amg *g, const Lsys *A) {
     }
 }
 
+/* AMGSolver::setup's coarsening loop (LinearSolver.hpp:516-551) on a given
+ * CSR matrix (rows sorted by column): buildAggregates + galerkinProduct until
+ * a level has at most 50 rows, stops coarsening, or max_levels levels exist.
+ * sizes[max_levels]; maps receives the aggregation map of every level that
+ * has one, concatenated.  Returns the level count. */
+int oracle_amg_levels(int n, const int *rowPtr, const int *colIdx, const double *values, int max_levels,
+                      int *sizes, int *maps) {
+    Csr A;
+    A.nRows = n;
+    A.rowPtr = xcalloc(n + 1, sizeof(int));
+    memcpy(A.rowPtr, rowPtr, sizeof(int) * (n + 1));
+    A.colIdx = xcalloc(rowPtr[n] > 0 ? rowPtr[n] : 1, sizeof(int));
+    memcpy(A.colIdx, colIdx, sizeof(int) * rowPtr[n]);
+    A.values = xcalloc(rowPtr[n] > 0 ? rowPtr[n] : 1, 8);
+    memcpy(A.values, values, 8 * (size_t)rowPtr[n]);
+    A.diag = xcalloc(n, 8);
+    for (int i = 0; i < n; ++i)
+        for (int j = rowPtr[i]; j < rowPtr[i + 1]; ++j)
+            if (colIdx[j] == i) A.diag[i] = values[j];
+    int levels = 1, at = 0;
+    sizes[0] = n;
+    while (levels < max_levels && A.nRows > 50) {
+        int *map = xcalloc(A.nRows, sizeof(int));
+        int nc = build_aggregates(&A, map);
+        if (nc == 0 || nc >= A.nRows) { free(map); break; }
+        memcpy(maps + at, map, sizeof(int) * A.nRows);
+        at += A.nRows;
+        Csr Cm = galerkin(&A, map, nc);
+        free(map);
+        csr_free(&A);
+        A = Cm;
+        sizes[levels++] = nc;
+    }
+    csr_free(&A);
+    return levels;
+}
+
 /* AMGSolver::vcycle (LinearSolver.hpp:553-589) */
 static void amg_vcycle(Amg *g, int level) {
     AmgLevel *lev = &g->lev[level];

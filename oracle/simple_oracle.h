@@ -47,6 +47,11 @@ void oracle_assemble(const btm_mesh *m, const btm_patch_bc *bcs, double nu,
                      const btm_state *st, const double *aP, const double *Smag,
                      double *diag, double *upper, double *lower, double *source, double *aP_out);
 
+/* AMGSolver::setup's coarsening (LinearSolver.hpp:516-551) on a CSR matrix:
+ * level sizes and the concatenated aggregation maps; returns the level count. */
+int oracle_amg_levels(int n, const int *rowPtr, const int *colIdx, const double *values, int max_levels,
+                      int *sizes, int *maps);
+
 /* LinearSystem::matvec (core/include/LinearSolver.hpp:68-77). */
 void oracle_matvec(int nC, int nIF, const int *own, const int *nbr, const double *diag,
                    const double *upper, const double *lower, const double *x, double *y);
