@@ -45,6 +45,12 @@ def lib():
         L.oracle_set_target_anisotropy.restype = None
         L.oracle_amg_levels.argtypes = [C.c_int, ip, ip, dp, C.c_int, ip, ip]
         L.oracle_amg_levels.restype = C.c_int
+        L.oracle_sst_point.argtypes = [dp, C.c_int, C.c_int, dp]
+        L.oracle_sst_point.restype = C.c_double
+        L.oracle_apply_bcs.argtypes = [C.POINTER(MeshDesc), C.POINTER(PatchBC), C.c_double, C.c_void_p]
+        L.oracle_apply_bcs.restype = None
+        L.oracle_transpose_stress.argtypes = [C.POINTER(MeshDesc), dp, dp, dp, C.c_int, dp]
+        L.oracle_transpose_stress.restype = None
         L.oracle_sst_fields.argtypes = [C.POINTER(MeshDesc), dp, C.c_int, C.c_double] + [dp] * 12
         L.oracle_assemble.argtypes = [C.POINTER(MeshDesc), C.POINTER(PatchBC), C.c_double,
                                       C.POINTER(Settings), dp, C.c_int, C.c_void_p, dp, dp,
@@ -259,3 +265,40 @@ def amg_levels(row_ptr, col_idx, values, max_levels=21):
         out.append(maps[at:at + sizes[l]].copy())
         at += sizes[l]
     return sizes[:nl].tolist(), out
+
+
+SST_POINT = {"production": 0, "production_omega": 1, "F1": 2, "F2": 3, "nut": 4}
+
+
+def sst_point(name, *args, coeffs=None, variant=0):
+    """One SSTModel point function of the restatement (see SST_POINT)."""
+    from rans_sst_py._types import COEFF_DEFAULTS
+    cf = np.ascontiguousarray(COEFF_DEFAULTS if coeffs is None else coeffs, np.float64)
+    a = np.ascontiguousarray(args + (0.0,) * (5 - len(args)), np.float64)
+    return float(lib().oracle_sst_point(_d(cf), int(variant), SST_POINT[name], _d(a)))
+
+
+def apply_bcs(mesh, bcs, nu, U, p=None, k=None, omega=None):
+    """The reference's four apply*BC functions on cell values: returns the
+    state dict with its boundary values (Ub, pb, kb, omegab) filled."""
+    m = mesh_arrays(mesh)
+    md, keep_m = mesh_desc(m)
+    bca, keep_b = bc_array(bcs)
+    nC, nB = int(m["cell_volume"].size), int(m["owner"].size) - int(m["n_internal"])
+    arrays, state = state_arrays(nC, nB)
+    arrays["U"][:] = U
+    for name, v in (("p", p), ("k", k), ("omega", omega)):
+        if v is not None:
+            arrays[name][:] = v
+    lib().oracle_apply_bcs(C.byref(md), bca, float(nu), C.cast(C.pointer(state), C.c_void_p))
+    return arrays
+
+
+def transpose_stress(mesh, coeff, U, Ub, comp):
+    """transposeStressSource (zero wall coefficient) of the restatement."""
+    m = mesh_arrays(mesh)
+    md, keep = mesh_desc(m)
+    a = [np.ascontiguousarray(v, np.float64) for v in (coeff, U, Ub)]
+    out = np.zeros(int(m["cell_volume"].size))
+    lib().oracle_transpose_stress(C.byref(md), *[_d(v) for v in a], int(comp), _d(out))
+    return out

@@ -522,6 +522,20 @@ static void amg_setup(Amg *g, const Lsys *A) {
     }
 }
 
+/* SSTModel point functions for known-answer checks: which = 0 production
+ * (nuT, S, k, omega), 1 productionOmega (nuT, S, k, omega), 2 F1 (k, omega,
+ * y, nu, CDkw+), 3 F2 (k, omega, y, nu), 4 eddy viscosity (k, omega, S, F2). */
+double oracle_sst_point(const double *coeffs, int variant, int which, const double *a) {
+    Sst s = sst_from(coeffs, variant);
+    switch (which) {
+        case 0: return production(&s, a[0], a[1], a[2], a[3]);
+        case 1: return productionOmega(&s, a[0], a[1], a[2], a[3]);
+        case 2: return computeF1(&s, a[0], a[1], a[2], a[3], a[4]);
+        case 3: return computeF2(&s, a[0], a[1], a[2], a[3]);
+        default: return eddyViscosity(&s, a[0], a[1], a[2], a[3]);
+    }
+}
+
 /* AMGSolver::setup's coarsening loop (LinearSolver.hpp:516-551) on a given
  * CSR matrix (rows sorted by column): buildAggregates + galerkinProduct until
  * a level has at most 50 rows, stops coarsening, or max_levels levels exist.
@@ -1402,6 +1416,49 @@ int oracle_solve(const btm_mesh *m, const btm_patch_bc *bcs, double nu, const bt
     fields_free(&f);
     solver_free(&S);
     return 0;
+}
+
+/* applyVelocityBC / applyPressureBC / applyKBC / applyOmegaBC
+ * (core/include/BoundaryCondition.hpp:196-342) on a state: boundary values
+ * from the cell values and the patch conditions, default SST coefficients
+ * (beta1 of the omega wall value). */
+void oracle_apply_bcs(const btm_mesh *m, const btm_patch_bc *bcs, double nu, btm_state *st) {
+    btm_settings s;
+    memset(&s, 0, sizeof s);
+    const double cf[11] = {0.85, 0.5, 0.075, 5.0 / 9.0, 1.0, 0.856, 0.0828, 0.44, 0.09, 0.31, 0.41};
+    Solver S;
+    solver_init(&S, m, bcs, nu, &s, cf, 0);
+    Fields f;
+    fields_alloc(&f, S.nC, S.nB > 0 ? S.nB : 1);
+    state_in(&f, st, S.nC, S.nB);
+    apply_velocity_bc(&S, &f);
+    apply_pressure_bc(&S, f.p, f.pb);
+    apply_k_bc(&S, &f);
+    apply_omega_bc(&S, &f, S.sst.beta1);
+    state_out(&f, st, S.nC, S.nB);
+    fields_free(&f);
+    solver_free(&S);
+}
+
+/* transposeStressSource with zero wall coefficient (StressOperators.hpp:312-365)
+ * for a coefficient field and a velocity with boundary values: src[n_cells]. */
+void oracle_transpose_stress(const btm_mesh *m, const double *coeff, const double *U, const double *Ub, int comp,
+                             double *src) {
+    btm_settings s;
+    memset(&s, 0, sizeof s);
+    const double cf[11] = {0.85, 0.5, 0.075, 5.0 / 9.0, 1.0, 0.856, 0.0828, 0.44, 0.09, 0.31, 0.41};
+    Solver S;
+    solver_init(&S, m, NULL, 1.0, &s, cf, 0);
+    Fields f;
+    fields_alloc(&f, S.nC, S.nB > 0 ? S.nB : 1);
+    for (int c = 0; c < S.nC; ++c) {
+        f.U[c] = mk(U[3 * c], U[3 * c + 1], U[3 * c + 2]);
+        f.nuT[c] = coeff[c];
+    }
+    for (int b = 0; b < S.nB; ++b) f.Ub[b] = mk(Ub[3 * b], Ub[3 * b + 1], Ub[3 * b + 2]);
+    transpose_stress(&S, &f, comp, src);
+    fields_free(&f);
+    solver_free(&S);
 }
 
 void oracle_green_gauss(const btm_mesh *m, const double *phi, const double *phib, double *grad) {

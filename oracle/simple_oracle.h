@@ -27,6 +27,15 @@ int oracle_solve(const btm_mesh *m, const btm_patch_bc *bcs, double nu, const bt
  * NULL switches the injection source off.  The array must outlive the calls. */
 void oracle_set_target_anisotropy(const double *b6);
 
+/* The four apply*BC functions (core/include/BoundaryCondition.hpp:196-342) on
+ * a state's cell values: fills its boundary values (default SST beta1). */
+void oracle_apply_bcs(const btm_mesh *m, const btm_patch_bc *bcs, double nu, btm_state *st);
+
+/* transposeStressSource with zero wall coefficient
+ * (core/include/StressOperators.hpp:312-365): src is n_cells. */
+void oracle_transpose_stress(const btm_mesh *m, const double *coeff, const double *U, const double *Ub, int comp,
+                             double *src);
+
 /* greenGaussGrad (core/include/Field.hpp:122-152): grad is n_cells*3. */
 void oracle_green_gauss(const btm_mesh *m, const double *phi, const double *phib, double *grad);
 
@@ -51,6 +60,11 @@ void oracle_assemble(const btm_mesh *m, const btm_patch_bc *bcs, double nu,
  * level sizes and the concatenated aggregation maps; returns the level count. */
 int oracle_amg_levels(int n, const int *rowPtr, const int *colIdx, const double *values, int max_levels,
                       int *sizes, int *maps);
+
+/* SSTModel point functions (core/src/SSTModel.cpp:9-96): which = 0
+ * production, 1 productionOmega, 2 F1, 3 F2, 4 eddy viscosity; arguments as
+ * the reference functions take them. */
+double oracle_sst_point(const double *coeffs, int variant, int which, const double *args);
 
 /* LinearSystem::matvec (core/include/LinearSolver.hpp:68-77). */
 void oracle_matvec(int nC, int nIF, const int *own, const int *nbr, const double *diag,
