@@ -166,3 +166,96 @@ def rel_l2(a, b) -> float:
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+_FOAM_BANNER = """/*--------------------------------*- C++ -*----------------------------------*\\
+  =========                 |
+  \\\\      /  F ield         | test fixture
+   \\\\    /   O peration     |
+    \\\\  /    A nd           |
+     \\\\/     M anipulation  |
+\\*---------------------------------------------------------------------------*/
+FoamFile
+{{
+    version     2.0;
+    format      ascii;
+    class       {cls};
+    location    "constant/polyMesh";
+    {note}object      {obj};
+}}
+// * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * * //
+
+"""
+
+
+def write_polymesh_block(path, nx, ny, nz, perturb=0.15, seed=3):
+    """An OpenFOAM ASCII polyMesh of an nx x ny x nz hex block on [0,2]x[0,1]x
+    [0,0.5] with interior nodes jittered by +-perturb of a cell size (seeded),
+    so interior faces are warped: internal faces in OpenFOAM upper-triangular
+    order, then patches inlet/outlet (patch), bottom/top (wall), front/back
+    (empty)."""
+    os.makedirs(path, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    hx, hy, hz = 2.0 / nx, 1.0 / ny, 0.5 / nz
+    nid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)  # noqa: E731
+    cid = lambda i, j, k: i + nx * (j + ny * k)               # noqa: E731
+    pts = np.zeros(((nx + 1) * (ny + 1) * (nz + 1), 3))
+    for k in range(nz + 1):
+        for j in range(ny + 1):
+            for i in range(nx + 1):
+                p = np.array([i * hx, j * hy, k * hz])
+                if 0 < i < nx and 0 < j < ny and 0 < k < nz:
+                    p += perturb * np.array([hx, hy, hz]) * rng.uniform(-1.0, 1.0, 3)
+                pts[nid(i, j, k)] = p
+    xf = lambda i, j, k: [nid(i, j, k), nid(i, j + 1, k), nid(i, j + 1, k + 1), nid(i, j, k + 1)]  # noqa: E731
+    yf = lambda i, j, k: [nid(i, j, k), nid(i, j, k + 1), nid(i + 1, j, k + 1), nid(i + 1, j, k)]  # noqa: E731
+    zf = lambda i, j, k: [nid(i, j, k), nid(i + 1, j, k), nid(i + 1, j + 1, k), nid(i, j + 1, k)]  # noqa: E731
+    faces, owner, neigh = [], [], []
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                c = cid(i, j, k)
+                if i + 1 < nx:
+                    faces.append(xf(i + 1, j, k)); owner.append(c); neigh.append(cid(i + 1, j, k))
+                if j + 1 < ny:
+                    faces.append(yf(i, j + 1, k)); owner.append(c); neigh.append(cid(i, j + 1, k))
+                if k + 1 < nz:
+                    faces.append(zf(i, j, k + 1)); owner.append(c); neigh.append(cid(i, j, k + 1))
+    patches = []
+
+    def patch(name, ptype, cells_faces):
+        start = len(faces)
+        for c, f in cells_faces:
+            faces.append(f); owner.append(c)
+        patches.append((name, ptype, len(faces) - start, start))
+
+    patch("inlet", "patch", [(cid(0, j, k), xf(0, j, k)[::-1]) for k in range(nz) for j in range(ny)])
+    patch("outlet", "patch", [(cid(nx - 1, j, k), xf(nx, j, k)) for k in range(nz) for j in range(ny)])
+    patch("bottom", "wall", [(cid(i, 0, k), yf(i, 0, k)[::-1]) for k in range(nz) for i in range(nx)])
+    patch("top", "wall", [(cid(i, ny - 1, k), yf(i, ny, k)) for k in range(nz) for i in range(nx)])
+    patch("front", "empty", [(cid(i, j, 0), zf(i, j, 0)[::-1]) for j in range(ny) for i in range(nx)])
+    patch("back", "empty", [(cid(i, j, nz - 1), zf(i, j, nz)) for j in range(ny) for i in range(nx)])
+    note = 'note        "nPoints:{} nCells:{} nFaces:{} nInternalFaces:{}";\n    '.format(
+        len(pts), nx * ny * nz, len(faces), len(neigh))
+
+    def write(name, cls, body, with_note=False):
+        with open(os.path.join(path, name), "w") as fh:
+            fh.write(_FOAM_BANNER.format(cls=cls, obj=name, note=note if with_note else ""))
+            fh.write(body)
+            fh.write("\n// ************************************************************************* //\n")
+
+    write("points", "vectorField", "\n{}\n(\n{}\n)\n".format(
+        len(pts), "\n".join("({!r} {!r} {!r})".format(*map(float, p)) for p in pts)))
+    write("faces", "faceList", "\n{}\n(\n{}\n)\n".format(
+        len(faces), "\n".join("4({} {} {} {})".format(*f) for f in faces)))
+    write("owner", "labelList", "\n{}\n(\n{}\n)\n".format(len(owner), "\n".join(map(str, owner))), True)
+    write("neighbour", "labelList", "\n{}\n(\n{}\n)\n".format(len(neigh), "\n".join(map(str, neigh))), True)
+    body = "\n{}\n(\n".format(len(patches))
+    for name, ptype, nf, start in patches:
+        body += "    {}\n    {{\n        type            {};\n".format(name, ptype)
+        if ptype == "wall":
+            body += "        inGroups        List<word> 1(wall);\n"
+        body += "        nFaces          {};\n        startFace       {};\n    }}\n".format(nf, start)
+    body += ")\n"
+    write("boundary", "polyBoundaryMesh", body)
+    return path

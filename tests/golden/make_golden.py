@@ -240,7 +240,30 @@ def make_chan180_inject():
     return out
 
 
-MAKERS = {"units": make_units, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
+FOAM_BLOCKS = {"b432": (4, 3, 2, 0.15, 3), "b653": (6, 5, 3, 0.2, 11)}
+
+
+def make_foam_blocks():
+    """The reference's OpenFOAM polyMesh loader (Mesh::loadOpenFOAM,
+    core/src/Mesh.cpp:50-265) on cases.write_polymesh_block fixtures: the
+    loaded topology and geometry."""
+    import tempfile
+    out = {}
+    keys = ("owner", "neighbour", "face_patch", "face_center", "face_normal", "face_area", "face_delta",
+            "face_d", "face_weight", "cell_center", "cell_volume", "cell_face_offset", "cell_faces", "nodes")
+    for tag, args in FOAM_BLOCKS.items():
+        with tempfile.TemporaryDirectory() as d:
+            path = cases.write_polymesh_block(os.path.join(d, "polyMesh"), *args)
+            r = rd.RefMesh.load(path).dump()
+        out[f"{tag}_args"] = np.array(args, dtype=np.float64)
+        out[f"{tag}_n_internal"] = np.array(r["n_internal"])
+        for k in keys:
+            out[f"{tag}_{k}"] = r[k]
+        out[f"{tag}_patch_names"] = np.frombuffer("\n".join(r["patch_names"]).encode(), np.uint8)
+    return out
+
+
+MAKERS = {"units": make_units, "foam_blocks": make_foam_blocks, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
           "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1,
           "chan180_inject_4x32": make_chan180_inject}
 # makers that extend an existing file instead of producing a new case
