@@ -1305,10 +1305,23 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             Job &J = jobs[i];
             btm::DevInst &I = J.S->inst;
             const btm_init *ini = inits ? &inits[i] : nullptr;
-            fill_inst(J.C, I, coeffs + 11 * (size_t)i, variants ? variants[i] : 0, ini);
-            if (ini && ini->mode == 1) {
-                if (!ini->warm) throw BtmError(BTM_ERR_ARG, "warm init without a state");
-                upload_state(J.C, I, ini->warm, st, stage);
+            if (ini && ini->mode == BTM_INIT_DEVICE) {
+                // continue from the state this slab holds: the kernel skips
+                // initialisation, turbEstablished and the z switch carry over
+                if (!J.S->hasState) throw BtmError(BTM_ERR_ARG, "device warm start before any solve of this slot");
+                const int solveZ = I.solveZ;
+                fill_inst(J.C, I, coeffs + 11 * (size_t)i, variants ? variants[i] : 0, nullptr);
+                I.initMode = 1;
+                I.turbEstIn = J.S->lastTurbEst;
+                I.solveZ = solveZ;
+            } else {
+                if (ini && ini->mode != BTM_INIT_COLD && ini->mode != BTM_INIT_WARM)
+                    throw BtmError(BTM_ERR_ARG, "unknown init mode");
+                fill_inst(J.C, I, coeffs + 11 * (size_t)i, variants ? variants[i] : 0, ini);
+                if (ini && ini->mode == BTM_INIT_WARM) {
+                    if (!ini->warm) throw BtmError(BTM_ERR_ARG, "warm init without a state");
+                    upload_state(J.C, I, ini->warm, st, stage);
+                }
             }
             I.hist = nullptr;
             I.histCap = 0;
@@ -1410,6 +1423,8 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             ck(cudaMemcpy(innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost), "status");
             ck(cudaMemcpy(lastv, I.outLast, sizeof lastv, cudaMemcpyDeviceToHost), "status");
             ck(cudaMemcpy(&errv, I.err, sizeof errv, cudaMemcpyDeviceToHost), "status");
+            J.S->hasState = errv == 0;
+            J.S->lastTurbEst = outv[5];
             const uint64_t *tns = times[i].data();
             if (hists) {
                 btm_history &h = hists[i];

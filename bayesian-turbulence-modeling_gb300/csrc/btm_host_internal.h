@@ -21,6 +21,8 @@ struct Slab {
     double *dObs = nullptr;   // observation outputs (allocated on first use)
     int obsCap = 0;
     double *dInj = nullptr;   // injection blend and tensor [9*nC] (allocated on first use)
+    bool hasState = false;    // a solve has left its final state in the slab
+    int lastTurbEst = 0;      // turbEstablished of that state
     btm::DevInst inst{};      // host copy with device pointers
 };
 

@@ -132,6 +132,8 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     if (int e = btm_host::ensure_device()) return e;
     if (C->settings.precision != BTM_PREC_FP64)
         return fail(BTM_ERR_ARG, "btm_solve_noalloc runs the FP64 engine only; set precision to fp64");
+    if (init && init->mode != BTM_INIT_COLD && init->mode != BTM_INIT_WARM)
+        return fail(BTM_ERR_ARG, "btm_solve_noalloc: the start is cold or warm from a state");
     if (C->dmesh.bTarget)
         return fail(BTM_ERR_ARG, "btm_solve_noalloc: Reynolds-stress injection needs per-instance work arrays; "
                                  "use btm_solve");

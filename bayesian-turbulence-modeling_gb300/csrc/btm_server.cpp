@@ -262,6 +262,8 @@ void btm_server_destroy(btm_server *S) {
 
 int btm_server_submit(btm_server *S, const btm_request *r) {
     if (!S || !r || !r->c || !r->coeffs) return sfail(BTM_ERR_ARG, "null argument");
+    if (r->init && r->init->mode != BTM_INIT_COLD && r->init->mode != BTM_INIT_WARM)
+        return sfail(BTM_ERR_ARG, "requests start cold, warm from a state, or from their tag");
     std::lock_guard<std::mutex> lock(S->mtx);
     try {
         btm_case *C = r->c;

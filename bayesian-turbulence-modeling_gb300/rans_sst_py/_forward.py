@@ -58,6 +58,11 @@ class SolveOutput:
 
 def _init_struct(init, keep):
     ini = BtmInit()
+    if isinstance(init, str):
+        if init != "device":
+            raise ValueError("init must be a dict, a state or 'device'")
+        ini.mode = 2    # BTM_INIT_DEVICE: continue from the state left on the device
+        return ini
     if init is None:
         init = {}
     if isinstance(init, dict) and "U" in init:
@@ -80,7 +85,9 @@ def solve_batch(cases: Sequence[Case], coeffs, variants=None, inits=None, want_s
     """Run len(cases) independent solves in one device launch.
 
     coeffs: (n, 11) SST constants; inits: per instance a dict with either
-    {"u", "p", "k", "omega"} (cold uniform start) or a full state dict (warm).
+    {"u", "p", "k", "omega"} (cold uniform start) or a full state dict (warm),
+    or "device": continue from the final state the previous solve left on the
+    device (the k-th instance of a case resumes the k-th instance's state).
     observe: evaluate the observation operator attached to a case
     (Case.set_observations) on the device; with want_state=False only the
     predictions and the log-likelihood leave the device.

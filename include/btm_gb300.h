@@ -158,7 +158,14 @@ typedef struct btm_settings {
 /* Initial state.  mode 0 = cold uniform start exactly as
  * SIMPLESolver::initUniform (SIMPLESolver.cpp:23-51); mode 1 = warm start from
  * the fields in `warm` (a state previously returned by a solve, as the
- * WarmStartCache does, ForwardModel.cpp:56-63). */
+ * WarmStartCache does, ForwardModel.cpp:56-63); mode 2 (BTM_INIT_DEVICE) =
+ * warm start from the final state of the previous solve still held on the
+ * device: the k-th instance of a case in a batch continues from what the
+ * k-th instance of that case left (no host copy; BTM_ERR_ARG when that slot
+ * has not solved yet).  Not a reference mode. */
+#define BTM_INIT_COLD   0
+#define BTM_INIT_WARM   1
+#define BTM_INIT_DEVICE 2
 typedef struct btm_state btm_state;
 typedef struct btm_init {
     int32_t mode;
