@@ -1267,6 +1267,22 @@ int btm_case_set_observations(btm_case *C, const btm_mesh *m, int32_t n, const b
     return BTM_OK;
 }
 
+// Per-call device buffers and events of btm_solve_batch, released when the
+// call returns or throws (cudaFree waits for work still using them).
+struct CallResources {
+    std::vector<void *> dev;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    CallResources() = default;
+    CallResources(const CallResources &) = delete;
+    CallResources &operator=(const CallResources &) = delete;
+    ~CallResources() {
+        for (void *p : dev)
+            if (p) cudaFree(p);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
 int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, const int32_t *variants,
                     const btm_init *inits, btm_state *outs, btm_history *hists) {
     if (n < 0 || (n > 0 && (!cases || !coeffs))) return fail(BTM_ERR_ARG, "null argument");
@@ -1301,6 +1317,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
         std::vector<int> blockIdx, gridIdx, mixIdx;
         std::vector<std::vector<double>> histBufs(n);
         std::vector<double *> histDev(n, nullptr);
+        CallResources res;
         for (int i = 0; i < n; ++i) {
             Job &J = jobs[i];
             btm::DevInst &I = J.S->inst;
@@ -1327,6 +1344,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             I.histCap = 0;
             if (hists && hists[i].residuals && hists[i].residual_capacity > 0) {
                 ck(cudaMalloc((void **)&histDev[i], sizeof(double) * 6 * hists[i].residual_capacity), "cudaMalloc(hist)");
+                res.dev.push_back(histDev[i]);
                 I.hist = histDev[i];
                 I.histCap = hists[i].residual_capacity;
             }
@@ -1344,9 +1362,9 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             }
         }
         // one persistent launch per engine for all block-mode instances
-        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-        ck(cudaEventCreate(&ev0), "event");
-        ck(cudaEventCreate(&ev1), "event");
+        ck(cudaEventCreate(&res.ev[0]), "event");
+        ck(cudaEventCreate(&res.ev[1]), "event");
+        cudaEvent_t ev0 = res.ev[0], ev1 = res.ev[1];
         btm::DevInst *dInsts = nullptr;
         const size_t nBlock = blockIdx.size() + mixIdx.size();
         if (nBlock > 0) {
@@ -1354,6 +1372,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             for (int i : blockIdx) arr.push_back(jobs[i].S->inst);
             for (int i : mixIdx) arr.push_back(jobs[i].S->inst);
             ck(cudaMalloc((void **)&dInsts, sizeof(btm::DevInst) * arr.size()), "cudaMalloc(insts)");
+            res.dev.push_back(dInsts);
             ck(cudaMemcpyAsync(dInsts, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
             ck(cudaEventRecord(ev0, st), "event");
             if (!blockIdx.empty()) {
@@ -1378,12 +1397,11 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
         } else {
             ck(cudaEventRecord(ev0, st), "event");
         }
-        std::vector<btm::DevInst *> gridPtrs;
         for (int i : gridIdx) {
             btm::DevInst *dI = nullptr;
             ck(cudaMalloc((void **)&dI, sizeof(btm::DevInst)), "cudaMalloc(inst)");
+            res.dev.push_back(dI);
             ck(cudaMemcpyAsync(dI, &jobs[i].S->inst, sizeof(btm::DevInst), cudaMemcpyHostToDevice, st), "inst");
-            gridPtrs.push_back(dI);
             int e;
             if (jobs[i].C->settings.precision == BTM_PREC_MIXED) {
                 int mb = 0;
@@ -1399,10 +1417,6 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
         cudaError_t se = cudaStreamSynchronize(st);
         float ms = 0.0f;
         if (se == cudaSuccess && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) g_launch_ms = ms;
-        cudaEventDestroy(ev0);
-        cudaEventDestroy(ev1);
-        if (dInsts) cudaFree(dInsts);
-        for (auto *p : gridPtrs) cudaFree(p);
         if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, std::string("solve: ") + cudaGetErrorString(se));
         // per-instance device timestamps: [8] start, [9] end of each solve
         std::vector<std::array<uint64_t, 10>> times(n);
@@ -1443,7 +1457,6 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                 if (histDev[i]) {
                     int rows = std::min(h.residual_capacity, outv[4]);
                     ck(cudaMemcpy(h.residuals, histDev[i], sizeof(double) * 6 * rows, cudaMemcpyDeviceToHost), "hist");
-                    cudaFree(histDev[i]);
                 }
                 download_obs(J.C, I, &h, st);
             }
