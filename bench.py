@@ -36,6 +36,7 @@ import json
 import multiprocessing as mp
 import os
 import statistics
+import tempfile
 import subprocess
 import sys
 import time
@@ -87,7 +88,10 @@ class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
     def __init__(self, gpu_index: int):
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples go next to the run's other outputs (BTM_CLOCKS_DIR, else
+        # the system temporary directory); the JSON line carries the summary
+        out_dir = os.environ.get("BTM_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"clocks_bench_{os.getpid()}.csv")
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
         self.proc = None
         self.gpu = gpu_index

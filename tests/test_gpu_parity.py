@@ -8,7 +8,7 @@ Tolerances (stated per test):
   * Krylov solves: same iterations, iterates within 1e-11 relative (parallel
     dot products round differently);
   * converged fields run to stagnation: 1e-8 relative L2 for U, k, omega, nu_t
-    (the spec bar); pressure 1e-8 of the dynamic pressure 0.5*max|U|^2
+    (the FP64 parity bar); pressure 1e-8 of the dynamic pressure 0.5*max|U|^2
     (on periodic domains p is a near-constant whose level is path-dependent).
 """
 import json
