@@ -111,7 +111,11 @@ struct btm_server {
 
 namespace {
 
-int64_t slab_bytes(const Slot &s) { return (int64_t)s.slab.bytes + (int64_t)s.slab.bytes32; }
+int64_t slab_bytes(const Slot &s) {
+    int64_t b = (int64_t)s.slab.bytes + (int64_t)s.slab.bytes32 + 8 * (int64_t)s.slab.obsCap;
+    if (s.slab.dInj && s.C) b += 72 * (int64_t)s.C->nC;   // injection blend and tensor, 9 doubles a cell
+    return b;
+}
 
 // Launch every PENDING slot: one persistent launch per engine and CTA size
 // (a request gets the CTA size it would get alone, so its result is the same
@@ -336,8 +340,10 @@ int btm_server_submit(btm_server *S, const btm_request *r) {
         }
         I.hist = nullptr;
         I.histCap = 0;
+        const int64_t held = slab_bytes(*slot);
         btm_host::ensure_obs(C, slot->slab, r->hist && r->hist->predictions);
         btm_host::ensure_inj(C, slot->slab);
+        S->used += slab_bytes(*slot) - held;   // observation / injection buffers allocated on first use
         S->hFlags[slot->flag] = 0;
         I.doneFlag = S->dFlags + slot->flag;
         sck(cudaMemsetAsync(I.barrier, 0, 512, S->copyStream), "memset control");
