@@ -240,6 +240,23 @@ def make_chan180_inject():
     return out
 
 
+def make_chan180_wallfn():
+    """Wall functions on (useWallFunctions: eddy viscosity at wall faces in the
+    momentum flux, the blended omega wall value, SIMPLESolver.cpp:115, 894-903)
+    on the Re_tau 180 4x32 channel: 50 iterations and 2000 iterations from
+    the cold start."""
+    m, bcs, nu, init = cases.periodic_channel(32, 180.0)
+    s = cases.channel_settings(50, 0.0)
+    s.use_wall_functions = True
+    mb, out = base_record(m, nu, s, init)
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("pin50", a, info, out)
+    s.max_iterations = 2000
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("pin2000", a, info, out)
+    return out
+
+
 FOAM_BLOCKS = {"b432": (4, 3, 2, 0.15, 3), "b653": (6, 5, 3, 0.2, 11)}
 
 
@@ -265,7 +282,7 @@ def make_foam_blocks():
 
 MAKERS = {"units": make_units, "foam_blocks": make_foam_blocks, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
           "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1,
-          "chan180_inject_4x32": make_chan180_inject}
+          "chan180_inject_4x32": make_chan180_inject, "chan180_wallfn_4x32": make_chan180_wallfn}
 # makers that extend an existing file instead of producing a new case
 EXTENDERS = {"bfs_perm_1920": add_bfs_continuation}
 

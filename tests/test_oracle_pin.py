@@ -191,3 +191,19 @@ def test_injection_pin(oracle, stage):
             assert h["final_iter"] == int(g["conv_final_iter"])
     for f in FIELDS:
         assert_same(st[f], g[f"{stage}_{f}"], 0.0 if SAME_PLATFORM else 1e-9)
+
+
+@pytest.mark.parametrize("stage,n", [("pin50", 50), ("pin2000", 2000)])
+def test_wall_function_pin(oracle, stage, n):
+    """useWallFunctions on (eddy viscosity at wall faces in the momentum flux,
+    the blended omega wall value; SIMPLESolver.cpp:115, 894-903)."""
+    g = cases.load_golden("chan180_wallfn_4x32")
+    m = mesh_from(g)
+    s = settings_from(g)
+    assert s.use_wall_functions
+    s.max_iterations, s.convergence_tol = n, 0.0
+    bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    st, h = oracle.solve(m, bcs, float(g["nu"]), s, cases.COEFF_DEFAULTS, 0, **init_from(g))
+    assert h["iterations_run"] == int(g[f"{stage}_iterations_run"])
+    for f in FIELDS:
+        assert_same(st[f], g[f"{stage}_{f}"], 0.0 if SAME_PLATFORM else 1e-9)
