@@ -1580,7 +1580,7 @@ int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t va
             case BTM_PHASE_SPMV: srcs = {I.v}; lens = {nC}; break;
             case BTM_PHASE_BICGSTAB:
             case BTM_PHASE_AMGPCG:
-            case 11: srcs = {I.pp, I.outLast}; lens = {nC, 4}; break;
+            case BTM_PHASE_PCG: srcs = {I.pp, I.outLast}; lens = {nC, 4}; break;
             default: throw BtmError(BTM_ERR_ARG, "unknown debug phase");
         }
         int64_t total = 0;
@@ -1605,6 +1605,7 @@ int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t va
 namespace btm_host {
 int ensure_device() { return ::ensure_device(); }
 void set_error(const std::string &msg) { g_err = msg; }
+void set_launch_ms(double ms) { g_launch_ms = ms; }
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
     ::fill_inst(C, I, coeffs, variant, init);
 }

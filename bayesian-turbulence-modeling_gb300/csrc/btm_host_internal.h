@@ -50,6 +50,8 @@ struct btm_case {
 namespace btm_host {
 int ensure_device();
 void set_error(const std::string &msg);
+// the value btm_last_launch_ms reports on this thread
+void set_launch_ms(double ms);
 // DevInst fields that do not depend on where the scratch lives (settings,
 // coefficients, initial-state mode, z-momentum switch)
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init);

@@ -16,8 +16,12 @@
 //     fit (mesh too large, or too many residual-history rows requested) is
 //     rejected with BTM_ERR_ARG and a message giving both sizes;
 //   * the first call on a device looks up the array's device address there
-//     (cudaGetSymbolAddress with that device current); make that first call
-//     before any stream capture;
+//     (cudaGetSymbolAddress with that device current) and creates the two
+//     CUDA events that time the launch; make that first call before any
+//     stream capture;
+//   * observables of the case (btm_case_set_observations) are evaluated into
+//     the same array when the caller passes hist->predictions, and only the
+//     residual-history rows the solve wrote are copied back;
 //   * every call on a device reuses the same array, which keeps the previous
 //     call's contents: the control words that must start at zero are cleared
 //     by each call; host calls are serialised by a mutex, but two processes
@@ -31,6 +35,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace {
 
@@ -61,8 +66,10 @@ cudaError_t scratch_address(void **out) {
 
 // Carve the DevInst arrays out of `base`; returns the bytes used.  With
 // base == nullptr only the size is computed.  Same arrays as the pooled slabs
-// of btm_solve; no grid-team reduction buffer (block mode only).
-size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, size_t &instOff, double **hist) {
+// of btm_solve; no grid-team reduction buffer (block mode only).  nObs > 0
+// adds the observation outputs (n_obs predictions and the log-likelihood).
+size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, int nObs, size_t &instOff, double **hist,
+             double **obs) {
     const int nC = C->nC, nIF = C->nIF, nB = C->nB;
     const int nc = C->dmesh.coarseDirect ? C->amgCoarseN : 1;
     auto up = [](size_t n) { return (n + 31) & ~size_t(31); };  // doubles, 256-byte granules
@@ -97,6 +104,7 @@ size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, size_t &ins
     I.gpart = take(2 * btm::kRedSlots);
     I.outLast = take(32);
     *hist = histRows > 0 ? take((size_t)6 * histRows) : nullptr;
+    *obs = nObs > 0 ? take((size_t)nObs + 1) : nullptr;
     char *ctl = b ? b + off : nullptr;
     I.barrier = (unsigned int *)ctl;
     I.err = (int32_t *)(ctl ? ctl + 64 : nullptr);
@@ -105,6 +113,25 @@ size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, size_t &ins
     I.outTime = (uint64_t *)(ctl ? ctl + 256 : nullptr);
     off += 512;
     return off;
+}
+
+// CUDA events that time the launch, created once per device (an event is not
+// device memory the caller accounts for)
+cudaEvent_t g_ev[kMaxDevices][2] = {};
+
+cudaError_t launch_events(cudaEvent_t *ev) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    for (int q = 0; q < 2; ++q) {
+        if (!g_ev[dev][q]) {
+            e = cudaEventCreate(&g_ev[dev][q]);
+            if (e != cudaSuccess) return e;
+        }
+        ev[q] = g_ev[dev][q];
+    }
+    return cudaSuccess;
 }
 
 cudaError_t put_strided(double *dst, const double *src, int n, cudaStream_t st) {
@@ -134,6 +161,7 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
         return fail(BTM_ERR_ARG, "btm_solve_noalloc runs the FP64 engine only; set precision to fp64");
     if (init && init->mode != BTM_INIT_COLD && init->mode != BTM_INIT_WARM)
         return fail(BTM_ERR_ARG, "btm_solve_noalloc: the start is cold or warm from a state");
+    if (init && init->mode == BTM_INIT_WARM && !init->warm) return fail(BTM_ERR_ARG, "warm init without a state");
     if (C->dmesh.bTarget)
         return fail(BTM_ERR_ARG, "btm_solve_noalloc: Reynolds-stress injection needs per-instance work arrays; "
                                  "use btm_solve");
@@ -142,10 +170,11 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
                                      " cells need the cooperative launch; use btm_solve");
     std::lock_guard<std::mutex> lock(g_noalloc_mtx);
     const int histRows = (hist && hist->residuals && hist->residual_capacity > 0) ? hist->residual_capacity : 0;
+    const int nObs = (hist && hist->predictions) ? C->dmesh.obs.n : 0;
     btm::DevInst I{};
     size_t instOff = 0;
-    double *dHist = nullptr;
-    const size_t need = carve(C, nullptr, I, histRows, instOff, &dHist);
+    double *dHist = nullptr, *dObs = nullptr;
+    const size_t need = carve(C, nullptr, I, histRows, nObs, instOff, &dHist, &dObs);
     if (need > kNoAllocScratchBytes)
         return fail(BTM_ERR_ARG, "btm_solve_noalloc: this solve needs " + std::to_string(need) +
                                      " bytes of scratch; the static scratch holds " +
@@ -153,24 +182,33 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     void *base = nullptr;
     cudaError_t e = scratch_address(&base);
     if (e != cudaSuccess) return fail(BTM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    cudaEvent_t ev[2];
+    e = launch_events(ev);
+    if (e != cudaSuccess) return fail(BTM_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
     std::memset(&I, 0, sizeof I);
-    carve(C, (char *)base, I, histRows, instOff, &dHist);
+    carve(C, (char *)base, I, histRows, nObs, instOff, &dHist, &dObs);
     btm_host::fill_inst(C, I, coeffs, variant, init);
     I.M = C->dMeshPtr;
     I.hist = dHist;
     I.histCap = histRows;
+    I.obsOut = dObs;
     cudaStream_t st = C->stream;
     btm::DevInst *dI = (btm::DevInst *)((char *)base + instOff);
+    // Once work is queued on `st`, every exit waits for it: the scratch is
+    // shared, and the next caller must not overlap copies still in flight.
+    auto drain = [&](int code) {
+        cudaStreamSynchronize(st);
+        return code;
+    };
     auto ck = [&](cudaError_t err, const char *what) -> bool {
         if (err == cudaSuccess) return true;
         btm_host::set_error(std::string(what) + ": " + cudaGetErrorString(err));
         return false;
     };
     // the previous call's control words must not leak into this one
-    if (!ck(cudaMemsetAsync(I.barrier, 0, 512, st), "clear control words")) return BTM_ERR_CUDA;
-    if (init && init->mode == 1) {
+    if (!ck(cudaMemsetAsync(I.barrier, 0, 512, st), "clear control words")) return drain(BTM_ERR_CUDA);
+    if (init && init->mode == BTM_INIT_WARM) {
         const btm_state *w = init->warm;
-        if (!w) return fail(BTM_ERR_ARG, "warm init without a state");
         const int nC = C->nC, nB = C->nB;
         bool ok = ck(put_strided(I.ux, w->U, nC, st), "upload") && ck(put_strided(I.uy, w->U + 1, nC, st), "upload") &&
                   ck(put_strided(I.uz, w->U + 2, nC, st), "upload") &&
@@ -184,11 +222,17 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
         double *bd[] = {I.pb, I.kb, I.omb};
         for (int q = 0; q < 3 && ok; ++q)
             if (nB > 0) ok = ck(cudaMemcpyAsync(bd[q], bs[q], sizeof(double) * nB, cudaMemcpyHostToDevice, st), "upload");
-        if (!ok) return BTM_ERR_CUDA;
+        if (!ok) return drain(BTM_ERR_CUDA);
     }
-    if (!ck(cudaMemcpyAsync(dI, &I, sizeof I, cudaMemcpyHostToDevice, st), "instance descriptor")) return BTM_ERR_CUDA;
+    if (!ck(cudaMemcpyAsync(dI, &I, sizeof I, cudaMemcpyHostToDevice, st), "instance descriptor"))
+        return drain(BTM_ERR_CUDA);
+    if (!ck(cudaEventRecord(ev[0], st), "event")) return drain(BTM_ERR_CUDA);
     int le = btm::engine_launch_block(dI, 1, btm_host::block_threads_for(C->nC), st);
-    if (le) return fail(BTM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+    if (le) {
+        btm_host::set_error(std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+        return drain(BTM_ERR_CUDA);
+    }
+    if (!ck(cudaEventRecord(ev[1], st), "event")) return drain(BTM_ERR_CUDA);
     int32_t outv[8] = {0};
     int64_t innerv[5] = {0, 0, 0, 0, 0};
     int32_t errv = 0;
@@ -217,12 +261,26 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
             if (hb[q] && nB > 0)
                 ok = ck(cudaMemcpyAsync(hb[q], db[q], sizeof(double) * nB, cudaMemcpyDeviceToHost, st), "download");
     }
-    if (ok && histRows > 0)
-        ok = ck(cudaMemcpyAsync(hist->residuals, dHist, sizeof(double) * 6 * histRows, cudaMemcpyDeviceToHost, st),
-                "history");
+    std::vector<double> obsv((size_t)nObs + 1, 0.0);
+    if (ok && nObs > 0)
+        ok = ck(cudaMemcpyAsync(obsv.data(), dObs, sizeof(double) * (nObs + 1), cudaMemcpyDeviceToHost, st),
+                "observations");
     cudaError_t se = cudaStreamSynchronize(st);
     if (!ok) return BTM_ERR_CUDA;
     if (se != cudaSuccess) return fail(BTM_ERR_CUDA, std::string("solve: ") + cudaGetErrorString(se));
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) btm_host::set_launch_ms(ms);
+    // Only the rows this solve wrote: the scratch still holds an earlier
+    // call's residuals beyond them, and the caller's rows past
+    // iterations_run stay untouched, as btm_solve leaves them.
+    const int rows = std::min(histRows, outv[4]);
+    if (rows > 0) {
+        if (!ck(cudaMemcpyAsync(hist->residuals, dHist, sizeof(double) * 6 * rows, cudaMemcpyDeviceToHost, st),
+                "history"))
+            return drain(BTM_ERR_CUDA);
+        se = cudaStreamSynchronize(st);
+        if (se != cudaSuccess) return fail(BTM_ERR_CUDA, std::string("history: ") + cudaGetErrorString(se));
+    }
     if (out) out->turb_established = outv[5];
     if (hist) {
         hist->status = outv[0];
@@ -237,6 +295,10 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
         for (int q = 0; q < 8; ++q) hist->phase_ms[q] = 1e-6 * (double)tns[q];
         hist->solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
         hist->finish_ms = hist->solve_ms;
+        if (nObs > 0) {
+            for (int q = 0; q < nObs; ++q) hist->predictions[q] = obsv[q];
+            hist->log_lik = obsv[nObs];
+        }
     }
     if (errv) return fail(BTM_ERR_TIMEOUT, "a bounded device wait timed out; the solve was abandoned");
     return BTM_OK;

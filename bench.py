@@ -24,10 +24,10 @@ launch.  After the timed steps the same batch runs once through the plain
 FP64 engine: `fp64_plain` is its throughput and `error_vs_fp64` the
 per-instance relative L2 of the mixed-precision fields against it.
 
-`--impl reference` times the CPU restatement of the reference algorithm
-(oracle/, or the reference built from its sources when present) on all host
-cores: a bounded sample of outer iterations per process, converted to solves/s
-with the measured iterations-per-converged-solve of the GPU FP64 path.
+`--impl reference` times the reference's CPU solver (the reference built from
+its sources when oracle/_ref holds it, else the C restatement in oracle/) on
+all host cores: complete cold solves of the same theta draw to the same 1e-8
+scaled residual, one per core per step, timed by the wall clock.
 """
 from __future__ import annotations
 
@@ -55,7 +55,6 @@ ACTIVE = [8, 0, 1, 9, 2, 10]
 NY, NX, RE_TAU, RATIO = 128, 4, 550.0, 1.08
 MAX_ITER, TOL = 60000, 1e-8
 INIT = dict(u=(20.0, 0.0, 0.0), p=0.0, k=1e-2, omega=10.0)
-CPU_SAMPLE_ITERS = 1500
 WORKLOAD = "theta256_channel4x128_re550"
 PRECISION = "mixed"
 
@@ -173,34 +172,85 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# ---- CPU side (oracle restatement on all host cores) -----------------------
-def _cpu_worker(args):
-    idx, n_iter = args
+# ---- CPU side (the reference algorithm on all host cores) -------------------
+_CPU_CTX = {}
+
+
+def _cpu_setup():
+    """Per-process state of a CPU worker: the case inputs, the theta set and
+    the solver the reference arm runs (the reference compiled from its own
+    sources when oracle/_ref holds it, else the C restatement in oracle/)."""
+    if _CPU_CTX:
+        return _CPU_CTX
     sys.path.insert(0, ROOT)
     sys.path.insert(0, PKG)
     from oracle import port
     m, bcs, nu, s = make_case_inputs()
     _, coeffs, valid = theta_set()
-    s.max_iterations, s.convergence_tol = n_iter, 0.0
-    ids = np.nonzero(valid)[0]
-    c = coeffs[ids[idx % len(ids)]]
+    _CPU_CTX.update(m=m, bcs=bcs, nu=nu, s=s, coeffs=coeffs, ids=np.nonzero(valid)[0], kind=reference_kind())
+    if _CPU_CTX["kind"] == "reference":
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import cases as tc
+        from oracle import refdriver as rd
+        path = os.path.join(tempfile.gettempdir(), f"btm_bench_mesh_{os.getpid()}.msh")
+        with open(path, "wb") as fh:
+            fh.write(tc.mesh_to_bytes(m))
+        # the reference loader reports on stdout; keep the JSON line alone there
+        saved = os.dup(1)
+        devnull = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(devnull, 1)
+        try:
+            rm = rd.RefMesh.load(path)
+            rm.wall_distance()
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+            os.close(devnull)
+        bca, keep = port.bc_array(bcs)
+        _CPU_CTX.update(rm=rm, bca=bca, keep=keep)
+    return _CPU_CTX
+
+
+def _cpu_solve(args):
+    """One solve of valid theta number j (cycled) on this host core: the
+    reference's ForwardModel path (cold uniform start, convergence test at
+    `tol`, at most `max_iter` outer iterations).  Returns (converged,
+    iterations, seconds)."""
+    j, max_iter, tol = args
+    from oracle import port
+    ctx = _cpu_setup()
+    s = ctx["s"].copy()
+    s.max_iterations, s.convergence_tol = max_iter, tol
+    c = ctx["coeffs"][ctx["ids"][j % len(ctx["ids"])]]
     t0 = time.perf_counter()
-    _, h = port.solve(m, bcs, nu, s, c, 0, **INIT)
-    return h["iterations_run"], time.perf_counter() - t0
+    if ctx["kind"] == "reference":
+        ini, _ = port.make_init(**INIT)
+        m = ctx["m"]
+        _, hist, _ = ctx["rm"].solve(ctx["bca"], ctx["nu"], port.settings_struct(s), c, 0, ini, m.n_cells(),
+                                     m.n_boundary_faces(), 0)
+        conv, its = int(hist.converged), int(hist.iterations_run)
+    else:
+        _, h = port.solve(ctx["m"], ctx["bcs"], ctx["nu"], s, c, 0, **INIT)
+        conv, its = int(h["converged"]), int(h["iterations_run"])
+    return conv, its, time.perf_counter() - t0
 
 
-def cpu_sample(n_proc: int, n_iter: int):
-    """Iterations/s of the CPU restatement, n_proc independent processes."""
+def _cpu_pool(n_proc):
     from oracle import port
     port.build()
-    ctx = mp.get_context("spawn")
+    return mp.get_context("spawn").Pool(n_proc)
+
+
+def cpu_converged_solves(pool, n_proc, n_solves, first=0):
+    """`n_solves` complete converged solves of consecutive valid theta on
+    `n_proc` host processes, scheduled dynamically (a core takes the next
+    theta as soon as its solve ends).  Returns the converged count, the wall
+    time, the per-solve latencies and the outer iterations per solve."""
+    jobs = [(first + j, MAX_ITER, TOL) for j in range(n_solves)]
     t0 = time.perf_counter()
-    with ctx.Pool(n_proc) as pool:
-        res = pool.map(_cpu_worker, [(i, n_iter) for i in range(n_proc)])
+    res = list(pool.imap_unordered(_cpu_solve, jobs))
     wall = time.perf_counter() - t0
-    iters = sum(r[0] for r in res)
-    per_proc_rate = statistics.mean(r[0] / r[1] for r in res)
-    return iters / wall, per_proc_rate, wall
+    return sum(r[0] for r in res), wall, [r[2] for r in res], [r[1] for r in res]
 
 
 def reference_kind():
@@ -255,27 +305,37 @@ def aggregate_ranks(world, dev_ms, wall_s, conv_counts):
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's own CPU solver (the build in
+    oracle/_ref when present, else its C restatement) on every host core.
+    One step = os.cpu_count() complete cold solves to the 1e-8 scaled
+    residual, one per core, of consecutive valid theta of the same 256-theta
+    draw (cycling through the 219 valid ones); the timed region is the wall
+    clock around all timed steps' solves, scheduled dynamically over the
+    cores.  Warm-up steps run one 100-iteration solve per process (process
+    start-up, imports, first calls)."""
     if rank != 0:
         return
     n_proc = os.cpu_count() or 1
     _, _, valid = theta_set()
-    iters_per_solve = args.iters_per_solve
-    values = []
-    for step in range(args.warmup + args.steps):
-        it_rate, per_proc, wall = cpu_sample(n_proc, CPU_SAMPLE_ITERS)
-        if step >= args.warmup:
-            values.append(it_rate / iters_per_solve)
-    value = statistics.mean(values)
+    with _cpu_pool(n_proc) as pool:
+        for _ in range(args.warmup):
+            pool.map(_cpu_solve, [(j, 100, 0.0) for j in range(n_proc)])
+        conv, wall, lat, its = cpu_converged_solves(pool, n_proc, args.steps * n_proc)
+    value = conv / wall
+    kind = reference_kind()
     line = {"metric": "converged RANS solves/sec", "value": value, "unit": "solves/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * N_THETA / max(value, 1e-30),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "n_theta": N_THETA, "n_valid": int(valid.sum()), "cells": NX * NY,
-                       "tol": TOL, "iters_per_converged_solve": iters_per_solve},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": n_proc, "kind": reference_kind(),
-                             "sample": f"{n_proc} processes x {CPU_SAMPLE_ITERS} outer iterations of the 4x128 "
-                                       f"channel per step, converted with {iters_per_solve} iterations per "
-                                       f"converged solve (extrapolated)"},
+            "config": {"workload": WORKLOAD, "precision": "fp64", "n_theta": N_THETA, "n_valid": int(valid.sum()),
+                       "cells": NX * NY, "tol": TOL, "solves_per_step": n_proc,
+                       "iters_per_converged_solve": float(np.mean(its))},
+            "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)), "p99": 1e3 * float(np.percentile(lat, 99)),
+                           "note": "wall time of each solve on its host core"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": n_proc, "kind": kind,
+                             "sample": f"{args.steps * n_proc} complete cold solves to the 1e-8 scaled residual "
+                                       f"({n_proc} per step, consecutive valid theta of the draw), "
+                                       f"{conv} converged, {wall:.1f} s wall on {n_proc} processes"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -411,14 +471,17 @@ def run_gpu(args, world, rank, local):
         fp["note"] = "mixed vs FP64, both run to stagnation (fixed-point error)"
         line["error_fixed_point"] = fp
     if rank == 0 and not args.no_cpu_baseline:
+        # the reference algorithm on every host core, timed on complete
+        # converged solves: one per core (about 10-20 s of CPU work)
         n_proc = os.cpu_count() or 1
-        it_rate, _, wall_cpu = cpu_sample(n_proc, CPU_SAMPLE_ITERS)
-        ips = fp64_iters or iters_per_solve
-        line["cpu_baseline"] = {"value": it_rate / ips, "unit": "solves/s", "cores": n_proc,
+        with _cpu_pool(n_proc) as pool:
+            pool.map(_cpu_solve, [(j, 100, 0.0) for j in range(n_proc)])
+            conv_cpu, wall_cpu, lat_cpu, its_cpu = cpu_converged_solves(pool, n_proc, n_proc)
+        line["cpu_baseline"] = {"value": conv_cpu / wall_cpu, "unit": "solves/s", "cores": n_proc,
                                 "kind": reference_kind(),
-                                "sample": f"{n_proc} processes x {CPU_SAMPLE_ITERS} outer iterations of the "
-                                          f"4x128 channel ({wall_cpu:.1f} s wall), converted with "
-                                          f"{ips:.0f} outer iterations per converged FP64 solve (extrapolated)"}
+                                "sample": f"{n_proc} complete cold solves to the 1e-8 scaled residual, one per "
+                                          f"host process ({conv_cpu} converged, {wall_cpu:.1f} s wall, "
+                                          f"{np.mean(its_cpu):.0f} outer iterations per solve)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -619,9 +682,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per launch, if measured")
-    ap.add_argument("--iters-per-solve", type=float, default=18128.0,
-                    help="reference arm: mean outer iterations per converged FP64 solve of the batch "
-                         "(measured on the GPU FP64 path of the same 219 theta)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="one launch of 304 instances capped at 200 outer iterations (for ncu captures)")

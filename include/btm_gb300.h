@@ -300,10 +300,13 @@ int btm_solve(btm_case *c, const double *coeffs, int32_t variant,
  * held from library load until process exit.  Meshes above 16384 cells (the
  * one-CTA limit) and solves whose scratch plus requested residual history
  * would exceed 16 MiB are rejected with BTM_ERR_ARG and a message.  The first call on each device looks up
- * the array's address with that device current: make it before any stream
- * capture.  Every call reuses the array (each call clears what must start at
- * zero); calls are serialised within a process, and calls from two processes
- * on one GPU at the same time would race. */
+ * the array's address with that device current and creates the two CUDA
+ * events that time the launch (btm_last_launch_ms reports it): make it before
+ * any stream capture.  Observables attached to the case are evaluated when
+ * hist->predictions is set, as btm_solve does.  Every call reuses the array
+ * (each call clears what must start at zero); calls are serialised within a
+ * process, and calls from two processes on one GPU at the same time would
+ * race. */
 int btm_solve_noalloc(btm_case *c, const double *coeffs, int32_t variant,
                       const btm_init *init, btm_state *out, btm_history *hist);
 
@@ -331,7 +334,19 @@ double btm_last_launch_ms(void);
 #define BTM_PHASE_SPMV          7   /* LinearSystem::matvec                    */
 #define BTM_PHASE_BICGSTAB      8   /* BiCGSTABSolver::solve                   */
 #define BTM_PHASE_AMGPCG        9   /* AMG-preconditioned CG                   */
-#define BTM_PHASE_ITER         10   /* Mesh::computeWallDistance (core/src/Mesh.cpp:345-373) on the device:
+#define BTM_PHASE_PCG          11   /* PCGSolver::solve (Jacobi-preconditioned CG) */
+
+/* Run one phase on one CTA with the state packed in `in` (the layout is
+ * documented beside the implementation in the host driver) and copy that
+ * phase's outputs to `out`.  The linear-solver phases read the system
+ * diag|upper|lower|source and the start vector x from `in` and return x
+ * followed by {iterations, final relative residual, initial residual,
+ * converged}. */
+int btm_debug_phase(btm_case *c, int32_t phase, const double *coeffs,
+                    int32_t variant, int32_t arg, const double *in, int64_t n_in,
+                    double *out, int64_t n_out);
+
+/* Mesh::computeWallDistance (core/src/Mesh.cpp:345-373) on the device:
  * out[c] = min over the wall face centres of |cell_centre[c] - w| (xyz
  * triples), 1e10 when there is no wall face; bit-identical to the reference.
  * Host buffers in and out. */
@@ -390,11 +405,6 @@ int btm_server_flush(btm_server *s);
 int btm_server_poll(btm_server *s, int32_t timeout_ms, int64_t *ids, int32_t cap, int32_t *n_done);
 /* counters: slots in use, slots allocated, bytes held, requests in flight */
 int btm_server_stats(const btm_server *s, int32_t *busy_slots, int32_t *slots, int64_t *bytes, int32_t *inflight);
-
-/* N full SIMPLE outer iterations          */
-int btm_debug_phase(btm_case *c, int32_t phase, const double *coeffs,
-                    int32_t variant, int32_t arg, const double *in, int64_t n_in,
-                    double *out, int64_t n_out);
 
 /* Test hook (no device needed): the host AMG hierarchy btm_case_create builds
  * for `mesh` - the reference's greedy aggregation (LinearSolver.hpp:407-443)

@@ -97,7 +97,7 @@ def make_c1():
     mb, out = base_record(m, nu, s, init)
     a, info, res = ref_solve(mb, m, bcs, nu, s, init, residual_capacity=60000)
     pack("conv", a, info, out)
-    out["conv_residuals"] = res[:info["iterations_run"]]
+    out["conv_residuals"] = res[:info["iterations_run"]:100]
     s.max_iterations, s.convergence_tol = 60000, 0.0
     a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
     pack("stag", a, info, out)
