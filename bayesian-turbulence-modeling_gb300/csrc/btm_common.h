@@ -69,6 +69,40 @@ struct ObsDev {
     const double *fArea, *fDelta, *fX;     // area, max(delta, 1e-20), face-centre x
 };
 
+// Level table of the reference-order AMG (ints, RamgWork::lev[level *
+// kRamgLevInts + field]): rows, offsets of the level's CSR row pointers,
+// entries, vectors, its map to the next level (-1: coarsest), the next
+// level's member offsets and members, its wavefront offsets, wavefront count
+// and entry count.
+enum : int { RL_N = 0, RL_PTR, RL_ENT, RL_VEC, RL_MAP, RL_MOFF, RL_MEM, RL_WFO, RL_NWF, RL_NNZ, kRamgLevInts };
+
+// Per-instance pools of the reference-order AMG (btm_ramg.cuh): coarse levels
+// rebuilt from the actual matrix at every solve.  rowPool = 2 nC + 64 coarse
+// rows, entPool = 3 nnz0 + 256 coarse entries (nnz0: level-0 CSR entries).
+struct RamgWork {
+    int32_t rowPool, entPool;
+    double *val;        // [entPool] coarse values
+    double *dg;         // [rowPool] coarse diagonals
+    double *rd;         // [nC + rowPool] reciprocal diagonals (level 0, then the coarse levels)
+    double *x, *b, *r;  // [rowPool] coarse vectors
+    double *cv;         // [nnz0] Galerkin contributions (scratch)
+    int32_t *ptr;       // [rowPool + 64] coarse row pointers, level after level
+    int32_t *col;       // [entPool]
+    int32_t *cj;        // [nnz0] Galerkin contribution columns (scratch)
+    int32_t *coff;      // [nC + 1] contribution offsets per coarse row (scratch)
+    int32_t *map;       // [nC + rowPool] aggregation map of every level
+    int32_t *memOff;    // [rowPool + 64] member offsets of every coarse level
+    int32_t *mem;       // [nC + rowPool] members (ascending) of every coarse row
+    int32_t *seed;      // [nC] claiming seed per row (-1: the row is a seed)
+    int32_t *aux, *aux2;// [nC] aggregate ids, depths, cursors (scratch)
+    int32_t *wfOff;     // [rowPool + 64] wavefront offsets of every coarse level
+    int32_t *wfRows;    // [rowPool]
+    int32_t *lev;       // [(kMaxLevels + 2) * 16] level table
+    uint64_t setupNs;   // device time spent in hierarchy setups this solve (leader's clock)
+    double *xs;         // shared-memory copy of every level's x (level 0 at 0, level l at
+                        // nC + its vector offset), or null when it does not fit
+};
+
 struct DevMesh {
     int32_t nC, nIF, nB, nF;
     int32_t is2d;          // all normals z == 0: the z-momentum system is identically zero
@@ -106,6 +140,13 @@ struct DevMesh {
     int32_t coarseDirect;      // coarsest level solved by its dense inverse
     AmgLevelDev lev[kMaxLevels];
     int64_t amgValTotal, amgVecTotal;
+    // level 0 of the reference-order AMG: entry ids of the lduToCSR layout
+    // (lev[0].rowPtr / colIdx) into diag|upper|lower, and the forward
+    // Gauss-Seidel wavefronts of that CSR (rows grouped by the depth of their
+    // lower-index neighbours)
+    const int32_t *r0Ent;
+    int32_t nnz0, nWf0;
+    const int32_t *wf0Off, *wf0Rows;
     DevGeom32 g32;
     ObsDev obs;
     // Reynolds-stress injection target anisotropy [6*nC] (xx yy zz xy xz yz
@@ -121,6 +162,7 @@ struct DevSettings {
     double bodyForce[3];
     double kMin, kMax, omegaMin, vonKarman;
     double alphaInj;       // blend factor of the Reynolds-stress injection source
+    int32_t refAmg;        // AMG solves use the reference-order AMG (btm_ramg.cuh)
 };
 
 // FP32 bulk of one mixed-precision instance: closure fields, gradients, the
@@ -198,11 +240,17 @@ struct DevInst {
     // served requests: completion flag in mapped host memory (null otherwise),
     // set by the leader after every output is written
     volatile int32_t *doneFlag;
+    // reference-order AMG pools (null unless S.refAmg)
+    RamgWork rg;
 };
 
 // engine entry points (btm_engine.cu)
 int engine_block_threads();
-int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream);
+// refAmg: some instance of the launch uses the reference-order AMG (the
+// kernel instantiated with that solver is launched); maxCells: the largest
+// mesh of the launch (sizes that kernel's shared-memory level vectors)
+int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream, bool refAmg = false,
+                        int maxCells = 0);
 int engine_launch_grid(DevInst *dInst, int blocks, void *stream);
 int engine_grid_blocks(int *blocks_out);
 int engine_launch_debug(DevInst *dInst, void *stream);

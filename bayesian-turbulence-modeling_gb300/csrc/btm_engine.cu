@@ -21,6 +21,7 @@
 #include "btm_bc.cuh"
 #include "btm_phases64.cuh"
 #include "btm_observe.cuh"
+#include "btm_ramg.cuh"
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -302,12 +303,96 @@ template <class T> struct AmgDriver {
     }
 };
 
+// AMGSolver::solve (LinearSolver.hpp:602-653) with the reference's own
+// hierarchy rebuilt from this system (btm_ramg.cuh); one CTA.  r = I.r,
+// z = I.s (the V-cycle's level-0 x), p = I.pv, Ap = I.v, level-0 residual I.t.
+__device__ __noinline__ SolveResult team_ramg_pcg(BlockTeamRef &tm, const DevMesh &M, DevInst &I, double *x,
+                                                  int maxIter, double tol) {
+    SolveResult res = {0, 0.0, 0.0, 0};
+    const int nC = M.nC;
+    const uint64_t t0 = tm.leader() ? globaltimer_ns() : 0;
+    const int nLev = ramg_setup(tm, M, I);
+    if (tm.leader()) I.rg.setupNs += globaltimer_ns() - t0;
+    double a0[1] = {0.0};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const double rc = I.src[c] - ldu_row<BlockTeamRef>(M, I, x, c);
+        I.r[c] = rc;
+        I.s[c] = 0.0;
+        a0[0] = fma(rc, rc, a0[0]);
+    }
+    tm.template sum<1>(a0);
+    const double r0 = sqrt(a0[0]);
+    res.initialRes = r0;
+    if (r0 < 1e-30) { res.converged = 1; return res; }
+    ramg_precondition(tm, M, I, nLev);
+    double a1[1] = {0.0};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const double z = I.s[c];
+        I.pv[c] = z;
+        a1[0] = fma(I.r[c], z, a1[0]);
+    }
+    tm.template sum<1>(a1);
+    double rz = a1[0];
+    for (int it = 0; it < maxIter; ++it) {
+        double a2[1] = {0.0};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const double ap = ldu_row<BlockTeamRef>(M, I, I.pv, c);
+            I.v[c] = ap;
+            a2[0] = fma(I.pv[c], ap, a2[0]);
+        }
+        tm.template sum<1>(a2);
+        const double pAp = a2[0];
+        if (fabs(pAp) < 1e-30) break;
+        const double alpha = rz / pAp;
+        double a3[1] = {0.0};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            x[c] = x[c] + alpha * I.pv[c];
+            const double rc = I.r[c] - alpha * I.v[c];
+            I.r[c] = rc;
+            I.s[c] = 0.0;
+            a3[0] = fma(rc, rc, a3[0]);
+        }
+        tm.template sum<1>(a3);
+        const double rn = sqrt(a3[0]);
+        res.iterations = it + 1;
+        res.finalRes = rn / r0;
+        if (res.finalRes < tol) { res.converged = 1; return res; }
+        ramg_precondition(tm, M, I, nLev);
+        double a4[1] = {0.0};
+        for (int c = tm.rank(); c < nC; c += tm.size()) a4[0] = fma(I.r[c], I.s[c], a4[0]);
+        tm.template sum<1>(a4);
+        const double rzNew = a4[0];
+        const double beta = rzNew / (rz + 1e-30);
+        for (int c = tm.rank(); c < nC; c += tm.size()) I.pv[c] = I.s[c] + beta * I.pv[c];
+        tm.sync();
+        rz = rzNew;
+    }
+    return res;
+}
+
+// The reference-order AMG runs in the kernel instantiated for BlockTeamRef
+// only (one CTA per instance); the other teams keep the per-case hierarchy.
+template <class T> struct RefAmg {
+    __device__ static bool on(const DevInst &) { return false; }
+    __device__ static SolveResult run(T &, const DevMesh &, DevInst &, double *, int, double) {
+        return {0, 0.0, 0.0, 0};
+    }
+};
+template <> struct RefAmg<BlockTeamRef> {
+    __device__ static bool on(const DevInst &I) { return I.S.refAmg != 0; }
+    __device__ static SolveResult run(BlockTeamRef &tm, const DevMesh &M, DevInst &I, double *x, int maxIter,
+                                      double tol) {
+        return team_ramg_pcg(tm, M, I, x, maxIter, tol);
+    }
+};
+
 // AMG-preconditioned CG (AMGSolver::solve, LinearSolver.hpp:602-653) on
 // (I.diag, I.upper, I.lower, I.src), x in place (the pressure correction
 // starts from zero).  Vectors: r = I.r, z = I.s (V-cycle level-0 x),
 // p = I.pv, Ap = I.v, V-cycle scratch I.t.
 template <class T>
 __device__ __noinline__ SolveResult team_amg_pcg(T &tm, const DevMesh &M, DevInst &I, double *x, int maxIter, double tol) {
+    if (RefAmg<T>::on(I)) return RefAmg<T>::run(tm, M, I, x, maxIter, tol);
     SolveResult res = {0, 0.0, 0.0, 0};
     const int nC = M.nC;
     AmgDriver<T>::setup(tm, M, I);
@@ -483,6 +568,7 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
     PhaseClock clk;
     clk.start(tm.leader());
     const uint64_t tStart = tm.leader() ? globaltimer_ns() : 0;
+    if (tm.leader()) I.rg.setupNs = 0;
 
     for (int iter = 0; iter < S.maxIter; ++iter) {
         if (!tm.ok()) break;
@@ -672,6 +758,11 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
         I.outLast[6] = normUx0;
         I.outLast[7] = normUy0;
         I.outLast[8] = normP0;
+        if (I.S.refAmg && I.S.pSolver == 3 && clk.acc[5] >= I.rg.setupNs) {
+            // hierarchy setups of the reference-order AMG count as AMG setup
+            clk.acc[5] -= I.rg.setupNs;
+            clk.acc[4] += I.rg.setupNs;
+        }
         for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
         I.outTime[8] = tStart;
         I.outTime[9] = globaltimer_ns();
@@ -705,6 +796,29 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_simple_block(DevInst *insts, i
 template __global__ void k_simple_block<256>(DevInst *, int);
 template __global__ void k_simple_block<512>(DevInst *, int);
 
+// The same for launches that contain instances with the reference-order AMG;
+// `xsCap` doubles of dynamic shared memory hold every level's x when they fit.
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_simple_block_ref(DevInst *insts, int n, int xsCap) {
+    __shared__ double red[2 * 32 * kRedSlots];
+    __shared__ DevMesh sM;
+    __shared__ DevInst sI;
+    extern __shared__ __align__(16) double xsm[];
+    if (blockIdx.x >= n) return;
+    if (threadIdx.x == 0) {
+        sI = insts[blockIdx.x];
+        sM = *sI.M;
+        sI.rg.xs = (sI.S.refAmg && (int64_t)sM.nC + sI.rg.rowPool <= xsCap) ? xsm : nullptr;
+    }
+    __syncthreads();
+    BlockTeamRef tm;
+    tm.red = red;
+    tm.buf = 0;
+    simple_solve(tm, sM, sI);
+}
+template __global__ void k_simple_block_ref<256>(DevInst *, int, int);
+template __global__ void k_simple_block_ref<512>(DevInst *, int, int);
+
 __global__ void __launch_bounds__(kThreads, 1) k_simple_grid(DevInst *inst) {
     __shared__ double red[2 * 32 * kRedSlots];
     __shared__ DevMesh sM;
@@ -730,7 +844,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_debug(DevInst *inst) {
         sM = *sI.M;
     }
     __syncthreads();
-    BlockTeam tm{red, 0};
+    BlockTeamRef tm;
+    tm.red = red;
+    tm.buf = 0;
     const DevMesh &M = sM;
     DevInst &I = sI;
     const int ph = I.dbgPhase, arg = I.dbgArg;
@@ -766,7 +882,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_debug(DevInst *inst) {
             phase_turb_cells(tm, M, I, ph - 5);
             break;
         case 7:  // v = A r
-            for (int c = tm.rank(); c < M.nC; c += tm.size()) I.v[c] = ldu_row<BlockTeam>(M, I, I.r, c);
+            for (int c = tm.rank(); c < M.nC; c += tm.size()) I.v[c] = ldu_row<BlockTeamRef>(M, I, I.r, c);
             break;
         case 8:  // BiCGSTAB on (diag,upper,lower,src), x = pp
             res = team_bicgstab(tm, M, I, I.pp, I.S.innerIter, I.S.innerTol);
@@ -778,6 +894,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_debug(DevInst *inst) {
             break;
         case 11:  // PCG (Jacobi)
             res = team_pcg(tm, M, I, I.pp, I.S.innerIter, I.S.innerTol);
+            break;
+        case 12:  // reference-order AMG hierarchy of (diag, upper, lower)
+            if (I.S.refAmg) res.iterations = ramg_setup(tm, M, I);
             break;
     }
     tm.sync();
@@ -834,12 +953,34 @@ int engine_wall_distance(const double *dCentres, int nC, const double *dWall, in
 // ---------------------------------------------------------------------------
 int engine_block_threads() { return kThreads; }
 
-int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream) {
+// Dynamic shared memory of the reference-order kernel for the level vectors
+// (every level's x: nC + 2 nC + 64 doubles) when they fit within this much.
+constexpr int kRamgXsBytes256 = 96 * 1024;    // two CTAs per SM
+constexpr int kRamgXsBytes512 = 192 * 1024;   // one CTA per SM
+
+int engine_launch_block(DevInst *dInsts, int n, int threads, void *stream, bool refAmg, int maxCells) {
     if (n <= 0) return 0;
-    if (threads == 256)
-        k_simple_block<256><<<n, 256, 0, (cudaStream_t)stream>>>(dInsts, n);
-    else
-        k_simple_block<512><<<n, 512, 0, (cudaStream_t)stream>>>(dInsts, n);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (refAmg) {
+        const int cap = threads == 256 ? kRamgXsBytes256 : kRamgXsBytes512;
+        // only what the level vectors need: the rest of the SM's shared
+        // memory / L1 stays L1, which holds level 0's matrix
+        const int64_t need = 8 * (3 * (int64_t)maxCells + 64);
+        const int bytes = need <= cap ? (int)need : 0;
+        cudaError_t e;
+        if (threads == 256) {
+            e = cudaFuncSetAttribute(k_simple_block_ref<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+            if (e != cudaSuccess) return (int)e;
+            k_simple_block_ref<256><<<n, 256, bytes, st>>>(dInsts, n, bytes / 8);
+        } else {
+            e = cudaFuncSetAttribute(k_simple_block_ref<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+            if (e != cudaSuccess) return (int)e;
+            k_simple_block_ref<512><<<n, 512, bytes, st>>>(dInsts, n, bytes / 8);
+        }
+    } else {
+        if (threads == 256) k_simple_block<256><<<n, 256, 0, st>>>(dInsts, n);
+        else k_simple_block<512><<<n, 512, 0, st>>>(dInsts, n);
+    }
     return (int)cudaGetLastError();
 }
 

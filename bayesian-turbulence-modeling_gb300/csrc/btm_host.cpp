@@ -343,6 +343,8 @@ void check_settings(const btm_settings &s) {
         throw BtmError(BTM_ERR_ARG, "relaxation factors must be positive");
     if (s.precision != BTM_PREC_FP64 && s.precision != BTM_PREC_MIXED)
         throw BtmError(BTM_ERR_ARG, "unknown precision code");
+    if (s.amg_order < BTM_AMG_AUTO || s.amg_order > BTM_AMG_MULTICOLOUR)
+        throw BtmError(BTM_ERR_ARG, "unknown amg_order code");
 }
 
 // hostOnly: stop after the (validated) host AMG hierarchy and return it
@@ -559,6 +561,31 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs, std::ve
     }
     for (auto &L : lv) colour(L);
     const int nL = (int)lv.size();
+    // forward Gauss-Seidel wavefronts of the level-0 CSR for the
+    // reference-order AMG: depth(i) = 1 + max depth of i's lower-index
+    // neighbours; rows grouped by depth, ascending within a group
+    std::vector<int> wf0Off, wf0Rows;
+    {
+        const HLevel &L0 = lv[0];
+        std::vector<int> depth(nC, 0);
+        int maxD = 0;
+        for (int i = 0; i < nC; ++i) {
+            int d = 0;
+            for (int j = L0.rowPtr[i]; j < L0.rowPtr[i + 1]; ++j)
+                if (L0.colIdx[j] < i) d = std::max(d, depth[L0.colIdx[j]] + 1);
+            depth[i] = d;
+            maxD = std::max(maxD, d);
+        }
+        const int nWf = nC > 0 ? maxD + 1 : 0;
+        wf0Off.assign(nWf + 1, 0);
+        for (int i = 0; i < nC; ++i) wf0Off[depth[i] + 1]++;
+        for (int w = 0; w < nWf; ++w) wf0Off[w + 1] += wf0Off[w];
+        wf0Rows.assign(nC, 0);
+        std::vector<int> cur(wf0Off.begin(), wf0Off.end() - (nWf > 0 ? 1 : 0));
+        for (int i = 0; i < nC; ++i) wf0Rows[cur[depth[i]]++] = i;
+        D.nWf0 = nWf;
+        D.nnz0 = (int32_t)L0.colIdx.size();
+    }
     D.nLevels = nL;
     D.coarseDirect = lv.back().n <= directMax ? 1 : 0;
     C->amgCoarseN = lv.back().n;
@@ -630,6 +657,7 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs, std::ve
     for (int b = 0; b < nB; ++b) baOverD[b] = barea[b] / bdC[b];
     const size_t o_aod = P(aOverD), o_baod = P(baOverD);
     struct LevOff { size_t rowPtr, colIdx, diagPos, gOff, gIdx, map, aggOff, aggMem, colorOff, colorRows; };
+    const size_t o_r0Ent = P(lv[0].entry), o_wf0Off = P(wf0Off), o_wf0Rows = P(wf0Rows);
     std::vector<LevOff> lo(nL);
     int64_t valTot = 0, vecTot = 0;
     for (int l = 0; l < nL; ++l) {
@@ -669,6 +697,9 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs, std::ve
     D.cbOff = I32(o_cbOff); D.cbFace = I32(o_cbFace); D.cbpOff = I32(o_cbpOff); D.cbpFace = I32(o_cbpFace);
     D.pinFace = I32(o_pin);
     D.aOverD = F64(o_aod);
+    D.r0Ent = I32(o_r0Ent);
+    D.wf0Off = I32(o_wf0Off);
+    D.wf0Rows = I32(o_wf0Rows);
     D.baOverD = F64(o_baod);
     auto F32 = [&](size_t at) { return (const float *)(base + at); };
     btm::DevGeom32 &G = D.g32;
@@ -824,6 +855,7 @@ void free_slab(Slab &S) {
     if (S.dptr32) cudaFree(S.dptr32);
     if (S.dObs) cudaFree(S.dObs);
     if (S.dInj) cudaFree(S.dInj);
+    if (S.dRamg) cudaFree(S.dRamg);
     S = Slab();
 }
 
@@ -834,6 +866,56 @@ void ensure_inj(btm_case *C, Slab &S) {
     }
     if (!S.dInj) ck(cudaMalloc((void **)&S.dInj, sizeof(double) * 9 * (size_t)C->nC), "cudaMalloc(injection)");
     S.inst.inj = S.dInj;
+}
+
+// Reference-order AMG (btm_ramg.cuh): used by FP64 solves on one-CTA meshes
+// when asked for, or automatically when the level-0 forward Gauss-Seidel
+// needs at most kAutoRefAmgWavefronts wavefronts (unstructured or renumbered
+// meshes; grid-ordered meshes would serialise into ~nx + ny wavefronts).
+constexpr int kAutoRefAmgWavefronts = 32;
+int use_ref_amg(const btm_case *C) {
+    const btm_settings &s = C->settings;
+    if (C->nC > block_max_cells() || s.precision != BTM_PREC_FP64) return 0;
+    if (s.pressure_solver != BTM_LS_AMG && s.momentum_solver != BTM_LS_AMG && s.turbulence_solver != BTM_LS_AMG)
+        return 0;
+    if (s.amg_order == BTM_AMG_REFERENCE) return 1;
+    if (s.amg_order == BTM_AMG_MULTICOLOUR) return 0;
+    return C->dmesh.nWf0 <= kAutoRefAmgWavefronts ? 1 : 0;
+}
+
+// Pools of the reference-order AMG carved from `base` (nullptr: size only);
+// returns the bytes used.
+size_t ramg_layout(const btm_case *C, char *base, btm::RamgWork &W) {
+    const int nC = C->nC, nnz0 = C->dmesh.nnz0;
+    const int R = 2 * nC + 64, E = 3 * nnz0 + 256;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off += (bytes + 255) & ~size_t(255);
+        return p;
+    };
+    auto D = [&](size_t n) { return (double *)take(8 * std::max<size_t>(n, 1)); };
+    auto I = [&](size_t n) { return (int32_t *)take(4 * std::max<size_t>(n, 1)); };
+    W.rowPool = R;
+    W.entPool = E;
+    W.val = D(E); W.dg = D(R); W.rd = D(nC + R); W.x = D(R); W.b = D(R); W.r = D(R); W.cv = D(nnz0);
+    W.ptr = I(R + 64); W.col = I(E); W.cj = I(nnz0); W.coff = I(nC + 1);
+    W.map = I(nC + R); W.memOff = I(R + 64); W.mem = I(nC + R);
+    W.seed = I(nC); W.aux = I(nC); W.aux2 = I(nC);
+    W.wfOff = I(R + 64); W.wfRows = I(R);
+    W.lev = I((btm::kMaxLevels + 2) * 16);
+    return off;
+}
+
+void ensure_ramg(btm_case *C, Slab &S) {
+    if (!S.inst.S.refAmg) return;
+    if (!S.dRamg) {
+        btm::RamgWork W{};
+        const size_t bytes = ramg_layout(C, nullptr, W);
+        ck(cudaMalloc(&S.dRamg, bytes), "cudaMalloc(reference AMG)");
+        S.bytesRamg = bytes;
+        ramg_layout(C, (char *)S.dRamg, S.inst.rg);
+    }
 }
 
 // aniso::sym3Eigenvalues + barycentricMargin (core/include/AnisotropyTools.hpp:23-67):
@@ -866,6 +948,7 @@ double barycentric_margin(const double *b) {
 
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init) {
     I.S = dev_settings(C->settings);
+    I.S.refAmg = use_ref_amg(C);
     I.obsOut = nullptr;
     I.inj = nullptr;
     I.nu = C->nu;
@@ -1353,6 +1436,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             if (mixed) ensure_mixed(J.C, *J.S);
             ensure_obs(J.C, *J.S, hists && hists[i].predictions);
             ensure_inj(J.C, *J.S);
+            ensure_ramg(J.C, *J.S);
             if (mixed && J.C->nC <= block_max_cells()) {
                 mixIdx.push_back(i);
             } else if (!mixed && J.C->nC <= block_max_cells()) {
@@ -1377,8 +1461,13 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             ck(cudaEventRecord(ev0, st), "event");
             if (!blockIdx.empty()) {
                 int maxCells = 0;
-                for (int i : blockIdx) maxCells = std::max(maxCells, jobs[i].C->nC);
-                int e = btm::engine_launch_block(dInsts, (int)blockIdx.size(), block_threads_for(maxCells), st);
+                bool refAmg = false;
+                for (int i : blockIdx) {
+                    maxCells = std::max(maxCells, jobs[i].C->nC);
+                    refAmg = refAmg || jobs[i].S->inst.S.refAmg;
+                }
+                int e = btm::engine_launch_block(dInsts, (int)blockIdx.size(), block_threads_for(maxCells), st, refAmg,
+                                                 maxCells);
                 if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
             }
             if (!mixIdx.empty()) {
@@ -1525,6 +1614,7 @@ int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t va
         btm_init ini{};
         ini.mode = 1;
         fill_inst(C, I, coeffs, variant, nullptr);
+        ensure_ramg(C, S);
         I.initMode = 1;
         I.dbgPhase = phase;
         I.dbgArg = arg;
@@ -1568,6 +1658,38 @@ int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t va
         cudaFree(dI);
         if (e) throw BtmError(BTM_ERR_CUDA, cudaGetErrorString((cudaError_t)e));
         if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, cudaGetErrorString(se));
+        if (phase == BTM_PHASE_AMG_LEVELS) {
+            if (!I.S.refAmg) throw BtmError(BTM_ERR_ARG, "the hierarchy phase needs amg_order = reference (FP64)");
+            const btm::RamgWork &W = I.rg;
+            double last[4];
+            ck(cudaMemcpy(last, I.outLast, sizeof last, cudaMemcpyDeviceToHost), "dbg out");
+            const int nLev = (int)last[0];
+            std::vector<int32_t> lev((btm::kMaxLevels + 2) * 16);
+            ck(cudaMemcpy(lev.data(), W.lev, 4 * lev.size(), cudaMemcpyDeviceToHost), "dbg out");
+            auto field = [&](int l, int f) { return lev[l * btm::kRamgLevInts + f]; };
+            std::vector<double> o;
+            o.push_back(nLev);
+            for (int l = 0; l < 21; ++l) o.push_back(l < nLev ? field(l, btm::RL_N) : 0);
+            auto ints = [&](const int32_t *d, int n) {
+                std::vector<int32_t> h(std::max(n, 1));
+                if (n > 0) ck(cudaMemcpy(h.data(), d, 4 * (size_t)n, cudaMemcpyDeviceToHost), "dbg out");
+                for (int q = 0; q < n; ++q) o.push_back(h[q]);
+            };
+            for (int l = 0; l + 1 < nLev; ++l) ints(W.map + field(l, btm::RL_MAP), field(l, btm::RL_N));
+            for (int l = 1; l < nLev; ++l) {
+                const int n = field(l, btm::RL_N), nnz = field(l, btm::RL_NNZ);
+                ints(W.ptr + field(l, btm::RL_PTR), n + 1);
+                ints(W.col + field(l, btm::RL_ENT), nnz);
+                std::vector<double> h(std::max(nnz, 1));
+                if (nnz > 0)
+                    ck(cudaMemcpy(h.data(), W.val + field(l, btm::RL_ENT), 8 * (size_t)nnz, cudaMemcpyDeviceToHost),
+                       "dbg out");
+                for (int q = 0; q < nnz; ++q) o.push_back(h[q]);
+            }
+            if ((int64_t)o.size() > n_out) throw BtmError(BTM_ERR_ARG, "debug output too small");
+            std::copy(o.begin(), o.end(), out);
+            return BTM_OK;
+        }
         std::vector<const double *> srcs;
         std::vector<int64_t> lens;
         switch (phase) {
@@ -1619,6 +1741,8 @@ void download_obs(btm_case *C, const btm::DevInst &I, btm_history *h, cudaStream
 }
 void free_slab(Slab &S) { ::free_slab(S); }
 void ensure_inj(btm_case *C, Slab &S) { ::ensure_inj(C, S); }
+void ensure_ramg(btm_case *C, Slab &S) { ::ensure_ramg(C, S); }
+size_t ramg_layout(const btm_case *C, char *base, btm::RamgWork &W) { return ::ramg_layout(C, base, W); }
 void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
                   std::vector<double> &stage) {
     ::upload_state(C, I, ws, st, stage);

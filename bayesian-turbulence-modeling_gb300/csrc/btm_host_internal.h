@@ -21,6 +21,8 @@ struct Slab {
     double *dObs = nullptr;   // observation outputs (allocated on first use)
     int obsCap = 0;
     double *dInj = nullptr;   // injection blend and tensor [9*nC] (allocated on first use)
+    void *dRamg = nullptr;    // reference-order AMG pools (allocated on first use)
+    size_t bytesRamg = 0;
     bool hasState = false;    // a solve has left its final state in the slab
     int lastTurbEst = 0;      // turbEstablished of that state
     btm::DevInst inst{};      // host copy with device pointers
@@ -69,6 +71,11 @@ void free_slab(Slab &S);
 // injection work of an instance: allocated and wired into S.inst when the
 // case has a target anisotropy, else S.inst.inj = null
 void ensure_inj(btm_case *C, Slab &S);
+// reference-order AMG pools of an instance, allocated and wired into S.inst.rg
+// when S.inst.S.refAmg (set by fill_inst)
+void ensure_ramg(btm_case *C, Slab &S);
+// the same pools carved from `base` (nullptr: size only); returns their bytes
+size_t ramg_layout(const btm_case *C, char *base, btm::RamgWork &W);
 // FP64 state between a caller's btm_state and a slab (synchronises `st`)
 void upload_state(btm_case *C, const btm::DevInst &I, const btm_state *ws, cudaStream_t st,
                   std::vector<double> &stage);

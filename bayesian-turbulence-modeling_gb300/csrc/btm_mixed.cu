@@ -1128,6 +1128,13 @@ constexpr int kMaxRefine = 2;          // FP64 refinement passes of the pressure
 constexpr double kPolishFactor = 100.0;
 constexpr int kStallWindow = 2000;     // stage 1 stalls when a window of this many iterations ...
 constexpr double kStallGain = 0.9;     // ... does not push its best residual below this times the last one
+// A cold start (or a warm start scaled by a cold solve's residual scales)
+// counts a window without gain as the FP32 floor only below this scaled
+// residual: early in a solve the residual is not monotone (the flow and the
+// turbulence fields adjust to each other) and a window can end above its
+// predecessor's best far from any floor, which would start the FP64 stage
+// thousands of iterations early.
+constexpr double kStallCeiling = 1e-4;
 constexpr int kAmgRefresh = 8;         // outer iterations between coarse-hierarchy refreshes
 
 template <class T>
@@ -1415,7 +1422,10 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
             winBest = smin(winBest, maxRes);
             bool stalled = false;
             if (iter + 1 - winStart >= kStallWindow) {
-                stalled = settled && !(winBest < kStallGain * bestRes);
+                // a warm start normalised by its own (small) first defects can
+                // sit on the FP32 floor at any scaled residual
+                const bool ownScale = I.initMode != 0 && !I.normFixed;
+                stalled = settled && !(winBest < kStallGain * bestRes) && (ownScale || winBest < kStallCeiling);
                 bestRes = smin(bestRes, winBest);
                 winBest = INFINITY;
                 winStart = iter + 1;

@@ -68,8 +68,8 @@ cudaError_t scratch_address(void **out) {
 // base == nullptr only the size is computed.  Same arrays as the pooled slabs
 // of btm_solve; no grid-team reduction buffer (block mode only).  nObs > 0
 // adds the observation outputs (n_obs predictions and the log-likelihood).
-size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, int nObs, size_t &instOff, double **hist,
-             double **obs) {
+size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, int nObs, bool refAmg, size_t &instOff,
+             double **hist, double **obs) {
     const int nC = C->nC, nIF = C->nIF, nB = C->nB;
     const int nc = C->dmesh.coarseDirect ? C->amgCoarseN : 1;
     auto up = [](size_t n) { return (n + 31) & ~size_t(31); };  // doubles, 256-byte granules
@@ -105,6 +105,7 @@ size_t carve(btm_case *C, char *base, btm::DevInst &I, int histRows, int nObs, s
     I.outLast = take(32);
     *hist = histRows > 0 ? take((size_t)6 * histRows) : nullptr;
     *obs = nObs > 0 ? take((size_t)nObs + 1) : nullptr;
+    if (refAmg) off += btm_host::ramg_layout(C, b ? b + off : nullptr, I.rg);
     char *ctl = b ? b + off : nullptr;
     I.barrier = (unsigned int *)ctl;
     I.err = (int32_t *)(ctl ? ctl + 64 : nullptr);
@@ -174,7 +175,10 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     btm::DevInst I{};
     size_t instOff = 0;
     double *dHist = nullptr, *dObs = nullptr;
-    const size_t need = carve(C, nullptr, I, histRows, nObs, instOff, &dHist, &dObs);
+    btm::DevInst probe{};
+    btm_host::fill_inst(C, probe, coeffs, variant, init);
+    const bool refAmg = probe.S.refAmg != 0;
+    const size_t need = carve(C, nullptr, I, histRows, nObs, refAmg, instOff, &dHist, &dObs);
     if (need > kNoAllocScratchBytes)
         return fail(BTM_ERR_ARG, "btm_solve_noalloc: this solve needs " + std::to_string(need) +
                                      " bytes of scratch; the static scratch holds " +
@@ -186,7 +190,7 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     e = launch_events(ev);
     if (e != cudaSuccess) return fail(BTM_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
     std::memset(&I, 0, sizeof I);
-    carve(C, (char *)base, I, histRows, nObs, instOff, &dHist, &dObs);
+    carve(C, (char *)base, I, histRows, nObs, refAmg, instOff, &dHist, &dObs);
     btm_host::fill_inst(C, I, coeffs, variant, init);
     I.M = C->dMeshPtr;
     I.hist = dHist;
@@ -227,7 +231,7 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     if (!ck(cudaMemcpyAsync(dI, &I, sizeof I, cudaMemcpyHostToDevice, st), "instance descriptor"))
         return drain(BTM_ERR_CUDA);
     if (!ck(cudaEventRecord(ev[0], st), "event")) return drain(BTM_ERR_CUDA);
-    int le = btm::engine_launch_block(dI, 1, btm_host::block_threads_for(C->nC), st);
+    int le = btm::engine_launch_block(dI, 1, btm_host::block_threads_for(C->nC), st, refAmg, C->nC);
     if (le) {
         btm_host::set_error(std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
         return drain(BTM_ERR_CUDA);

@@ -114,6 +114,7 @@ namespace {
 int64_t slab_bytes(const Slot &s) {
     int64_t b = (int64_t)s.slab.bytes + (int64_t)s.slab.bytes32 + 8 * (int64_t)s.slab.obsCap;
     if (s.slab.dInj && s.C) b += 72 * (int64_t)s.C->nC;   // injection blend and tensor, 9 doubles a cell
+    b += (int64_t)s.slab.bytesRamg;                        // reference-order AMG pools
     return b;
 }
 
@@ -137,9 +138,11 @@ void dispatch(btm_server *S) {
         std::vector<btm::DevInst> arr;
         int maxCells = 0;
         size_t smem = 0;
+        bool refAmg = false;
         for (Slot *s : group) {
             arr.push_back(s->slab.inst);
             maxCells = std::max(maxCells, s->C->nC);
+            refAmg = refAmg || s->slab.inst.S.refAmg;
             if (s->mixed)
                 smem = std::max(smem, btm::mixed_smem_bytes(s->C->nC, s->C->nIF, s->C->amgVecTotal, s->C->amgValTotal,
                                                              s->C->dmesh.coarseDirect ? s->C->amgCoarseN : 1));
@@ -155,7 +158,7 @@ void dispatch(btm_server *S) {
         sck(cudaMallocAsync((void **)&d, sizeof(btm::DevInst) * arr.size(), st), "cudaMallocAsync(insts)");
         sck(cudaMemcpyAsync(d, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
         const int threads = btm_host::block_threads_for(maxCells);
-        int e = engine == 0 ? btm::engine_launch_block(d, (int)arr.size(), threads, st)
+        int e = engine == 0 ? btm::engine_launch_block(d, (int)arr.size(), threads, st, refAmg, maxCells)
                             : btm::mixed_launch_block(d, (int)arr.size(), threads, smem, st);
         if (e) throw SrvError(BTM_ERR_CUDA, std::string("server launch: ") + cudaGetErrorString((cudaError_t)e));
         sck(cudaFreeAsync(d, st), "cudaFreeAsync(insts)");
@@ -343,7 +346,8 @@ int btm_server_submit(btm_server *S, const btm_request *r) {
         const int64_t held = slab_bytes(*slot);
         btm_host::ensure_obs(C, slot->slab, r->hist && r->hist->predictions);
         btm_host::ensure_inj(C, slot->slab);
-        S->used += slab_bytes(*slot) - held;   // observation / injection buffers allocated on first use
+        btm_host::ensure_ramg(C, slot->slab);
+        S->used += slab_bytes(*slot) - held;   // buffers allocated on first use
         S->hFlags[slot->flag] = 0;
         I.doneFlag = S->dFlags + slot->flag;
         sck(cudaMemsetAsync(I.barrier, 0, 512, S->copyStream), "memset control");

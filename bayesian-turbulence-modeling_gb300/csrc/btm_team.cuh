@@ -157,6 +157,12 @@ struct BlockTeam {
     }
 };
 
+// One CTA per instance whose AMG solves use the reference-order AMG
+// (btm_ramg.cuh).  A distinct type so that only the kernel instantiated for
+// it carries that solver in its call graph (the plain kernel keeps its
+// register allocation).
+struct BlockTeamRef : BlockTeam {};
+
 struct GridTeam {
     double *red;            // shared [2][32][kRedSlots]
     int buf;
@@ -310,6 +316,7 @@ template <> struct Ld<BlockTeam> {
     __device__ __forceinline__ static double f(const double *p) { return *p; }
     __device__ __forceinline__ static float f(const float *p) { return *p; }
 };
+template <> struct Ld<BlockTeamRef> : Ld<BlockTeam> {};
 template <> struct Ld<GridTeam> {
     __device__ __forceinline__ static double f(const double *p) { return __ldcg(p); }
     __device__ __forceinline__ static float f(const float *p) { return __ldcg(p); }

@@ -46,7 +46,8 @@ class BtmSettings(C.Structure):
                 ("omega_min", C.c_double), ("use_wall_functions", C.c_int32),
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
-                ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double)]
+                ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double),
+                ("amg_order", C.c_int32)]
 
 
 class BtmState(C.Structure):
@@ -77,8 +78,9 @@ class BtmObservable(C.Structure):
 
 SOLVER_CODES = {"PCG": 0, "BiCGSTAB": 1, "GaussSeidel": 2, "AMG": 3}
 PRECISION_CODES = {"fp64": 0, "mixed": 1}
+AMG_ORDER_CODES = {"auto": 0, "reference": 1, "multicolour": 2}
 PHASES = {"grad": 1, "sst": 2, "momentum": 3, "pressure": 4, "k": 5, "omega": 6, "spmv": 7,
-          "bicgstab": 8, "amgpcg": 9, "pcg": 11}
+          "bicgstab": 8, "amgpcg": 9, "pcg": 11, "amg_levels": 12}
 
 _lib = None
 _lock = threading.Lock()
@@ -220,6 +222,10 @@ def settings_struct(s) -> BtmSettings:
         raise ValueError(f"precision must be one of {sorted(PRECISION_CODES)}, not {prec!r}")
     st.precision = PRECISION_CODES[prec]
     st.alpha_injection = float(getattr(s, "alpha_injection", 0.3))
+    order = getattr(s, "amg_order", "auto")
+    if order not in AMG_ORDER_CODES:
+        raise ValueError(f"amg_order must be one of {sorted(AMG_ORDER_CODES)}, not {order!r}")
+    st.amg_order = AMG_ORDER_CODES[order]
     return st
 
 
@@ -245,6 +251,23 @@ def state_struct(st: dict) -> BtmState:
         setattr(s, k, dptr(a))
     s.turb_established = int(st.get("turb_established", 0))
     return s
+
+
+def observable_structs(mesh, obs_op):
+    """The btm_observable records of an ObservationOperator (None: none), in
+    its order, patches resolved to indices of `mesh`; returns (array, n)."""
+    items = obs_op.observables() if obs_op is not None else []
+    arr = (BtmObservable * max(len(items), 1))()
+    for i, o in enumerate(items):
+        a = arr[i]
+        a.type = int(o.type)
+        a.patch = mesh.patch_by_name(o.patchName) if o.patchName else -1
+        a.component = int(o.component)
+        a.location[0], a.location[1], a.location[2] = o.location.x, o.location.y, o.location.z
+        a.observed, a.sigma_obs, a.sigma_model = o.observed, o.sigma_obs, o.sigma_model
+        a.ref_area, a.ref_velocity = o.referenceArea, o.refVelocity
+        a.ref_pressure, a.ref_density = o.refPressure, o.refDensity
+    return arr, len(items)
 
 
 class Case:
@@ -290,20 +313,10 @@ class Case:
         """Attach an ObservationOperator (None: detach): every later solve of
         this case evaluates its observables and the log-likelihood on the
         device (btm_case_set_observations)."""
-        items = obs_op.observables() if obs_op is not None else []
-        arr = (BtmObservable * max(len(items), 1))()
         mesh = self._mesh
-        for i, o in enumerate(items):
-            a = arr[i]
-            a.type = int(o.type)
-            a.patch = mesh.patch_by_name(o.patchName) if o.patchName else -1
-            a.component = int(o.component)
-            a.location[0], a.location[1], a.location[2] = o.location.x, o.location.y, o.location.z
-            a.observed, a.sigma_obs, a.sigma_model = o.observed, o.sigma_obs, o.sigma_model
-            a.ref_area, a.ref_velocity = o.referenceArea, o.refVelocity
-            a.ref_pressure, a.ref_density = o.refPressure, o.refDensity
+        arr, n = observable_structs(mesh, obs_op)
         ms, keep = mesh_struct(mesh)
-        check(self._L.btm_case_set_observations(self.h, C.byref(ms), len(items), arr))
+        check(self._L.btm_case_set_observations(self.h, C.byref(ms), n, arr))
         self.n_obs = len(items)
 
     def set_target_anisotropy(self, b6):

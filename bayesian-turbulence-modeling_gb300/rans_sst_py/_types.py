@@ -182,9 +182,11 @@ class InferenceParameterSet:
 class SolverSettings:
     """SolverSettings (core/include/FlowFields.hpp:53-132) with the snake_case
     attribute names of Bindings.cpp:414-441.  pressure_solver /
-    momentum_solver / turbulence_solver are also settable here, and
+    momentum_solver / turbulence_solver are also settable here,
     `precision` ("fp64", the reference's arithmetic, or "mixed": FP32 bulk
-    with FP64 state, defects and refinement) selects the device engine."""
+    with FP64 state, defects and refinement) selects the device engine, and
+    `amg_order` ("auto", "reference" or "multicolour") the form of the FP64
+    engine's AMG-preconditioned CG (BTM_AMG_* in the C header)."""
 
     def __init__(self):
         self.max_iterations = 500
@@ -216,6 +218,7 @@ class SolverSettings:
         self.wall_fn_E = 9.0
         self.sst_variant = 0
         self.precision = "fp64"
+        self.amg_order = "auto"
 
     def copy(self) -> "SolverSettings":
         s = SolverSettings()

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BTM_ABI_VERSION 4
+#define BTM_ABI_VERSION 5
 
 /* ---- status codes -------------------------------------------------------- */
 #define BTM_OK              0
@@ -83,6 +83,24 @@ extern "C" {
  * built from FP32-rounded coefficients.  No reference counterpart. */
 #define BTM_PREC_FP64       0
 #define BTM_PREC_MIXED      1
+
+/* ---- form of the AMG-preconditioned CG in the FP64 engine -------------------
+ * REFERENCE: the reference's AMGSolver (LinearSolver.hpp:497-656): the
+ * hierarchy is rebuilt from the actual matrix at every solve by the
+ * reference's greedy aggregation (bit-identical maps) and Galerkin product,
+ * smoothed by forward Gauss-Seidel in row order (2 + 2 sweeps, 50 on the
+ * coarsest level of at most 50 rows), evaluated in parallel by wavefronts of
+ * the row-order dependencies.  MULTICOLOUR: the aggregation of the geometric
+ * pressure Laplacian once per case, multicolour symmetric Gauss-Seidel and a
+ * dense coarsest inverse (fewer dependent steps on meshes numbered in grid
+ * order).  AUTO: REFERENCE for FP64 solves on meshes of at most 16384 cells
+ * whose level-0 Gauss-Seidel needs at most 32 wavefronts (unstructured or
+ * renumbered meshes), MULTICOLOUR otherwise.  Meshes above 16384 cells and the
+ * mixed-precision engine always use their own hierarchy.  Not a reference
+ * field. */
+#define BTM_AMG_AUTO        0
+#define BTM_AMG_REFERENCE   1
+#define BTM_AMG_MULTICOLOUR 2
 
 /* ---- SST closure variants (core/include/SSTModel.hpp:48) ------------------- */
 #define BTM_SST_FULL        0
@@ -153,6 +171,7 @@ typedef struct btm_settings {
     int32_t precision;             /* BTM_PREC_*; not a reference field */
     double  alpha_injection;       /* blend factor of the Reynolds-stress
                                       injection source (alphaInjection) */
+    int32_t amg_order;             /* BTM_AMG_*; not a reference field */
 } btm_settings;
 
 /* Initial state.  mode 0 = cold uniform start exactly as
@@ -335,6 +354,11 @@ double btm_last_launch_ms(void);
 #define BTM_PHASE_BICGSTAB      8   /* BiCGSTABSolver::solve                   */
 #define BTM_PHASE_AMGPCG        9   /* AMG-preconditioned CG                   */
 #define BTM_PHASE_PCG          11   /* PCGSolver::solve (Jacobi-preconditioned CG) */
+#define BTM_PHASE_AMG_LEVELS   12   /* AMGSolver::setup in the reference order (needs
+                                       amg_order = BTM_AMG_REFERENCE): out = level
+                                       count, 21 level sizes, the aggregation map of
+                                       every level but the coarsest, then per coarse
+                                       level its CSR row pointers, columns, values */
 
 /* Run one phase on one CTA with the state packed in `in` (the layout is
  * documented beside the implementation in the host driver) and copy that

@@ -41,7 +41,8 @@ class Settings(C.Structure):
                 ("omega_min", C.c_double), ("use_wall_functions", C.c_int32),
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
-                ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double)]
+                ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double),
+                ("amg_order", C.c_int32)]
 
 
 class State(C.Structure):

@@ -13,8 +13,9 @@
 // (core/include/BoundaryCondition.hpp:36-190), SIMPLESolver
 // (incompressible/include/SIMPLESolver.hpp:18-27), the header-only linear
 // solvers (core/include/LinearSolver.hpp:147-656), greenGaussGrad
-// (core/include/Field.hpp:122-152) and SSTModel::computeFields
-// (core/src/SSTModel.cpp:122-172).
+// (core/include/Field.hpp:122-152), SSTModel::computeFields
+// (core/src/SSTModel.cpp:122-172) and the header-only ObservationOperator
+// (core/include/ObservationOperator.hpp:46-378).
 
 #include "Mesh.hpp"
 #include "Field.hpp"
@@ -24,6 +25,7 @@
 #include "SSTModel.hpp"
 #include "SIMPLESolver.hpp"
 #include "InferenceParameters.hpp"
+#include "ObservationOperator.hpp"
 
 #include "../include/btm_gb300.h"
 
@@ -352,6 +354,60 @@ int ref_solve(void *mp, const btm_patch_bc *bcs, double nu, const btm_settings *
                 }
             }
         }
+        return 0;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+// ObservationOperator::evaluate and ::logLikelihood
+// (core/include/ObservationOperator.hpp:186-378) on a given state: the n
+// observables described by `obs` (patches by index into the mesh's patch
+// list) are added through the operator's own add* methods, in order.
+int ref_observe(void *mp, int n, const btm_observable *obs, double nu, const btm_state *st, double *pred,
+                double *loglik) {
+    try {
+        const Mesh &m = *static_cast<Mesh *>(mp);
+        ObservationOperator op;
+        for (int i = 0; i < n; ++i) {
+            const btm_observable &o = obs[i];
+            const std::string patch = (o.patch >= 0 && o.patch < m.nPatches()) ? m.patch(o.patch).name : "";
+            const Vec3 loc(o.location[0], o.location[1], o.location[2]);
+            switch (o.type) {
+                case BTM_OBS_DRAG:
+                    op.addDrag(patch, o.observed, o.sigma_obs, o.ref_area, o.ref_velocity, o.sigma_model);
+                    break;
+                case BTM_OBS_PRESSURE_TAP:
+                    op.addPressureTap(loc, o.observed, o.sigma_obs, o.ref_velocity, o.sigma_model, o.ref_pressure,
+                                      o.ref_density);
+                    break;
+                case BTM_OBS_VELOCITY:
+                    op.addVelocityProfile(loc, o.component, o.observed, o.sigma_obs, o.sigma_model);
+                    break;
+                case BTM_OBS_SKIN_FRICTION:
+                    op.addSkinFriction(patch, loc, o.observed, o.sigma_obs, o.ref_velocity, o.sigma_model);
+                    break;
+                case BTM_OBS_SEPARATION:
+                    op.addSeparationPoint(patch, o.observed, o.sigma_obs, o.sigma_model);
+                    break;
+                case BTM_OBS_REATTACHMENT:
+                    op.addReattachmentLength(patch, o.observed, o.sigma_obs, o.sigma_model);
+                    break;
+                default:
+                    g_err = "unknown observable type";
+                    return -1;
+            }
+        }
+        FlowFields f(m);
+        vecIn(f.U, st->U, st->Ub);
+        scalarIn(f.p, st->p, st->pb);
+        scalarIn(f.k, st->k, st->kb);
+        scalarIn(f.omega, st->omega, st->omegab);
+        if (st->nuT) scalarIn(f.nuT, st->nuT, nullptr);
+        const std::vector<double> h = op.evaluate(m, f, nu);
+        for (int i = 0; i < n; ++i) pred[i] = h[i];
+        *loglik = op.logLikelihood(m, f, nu);
         return 0;
     } catch (const std::exception &e) {
         g_err = e.what();

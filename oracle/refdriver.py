@@ -58,6 +58,7 @@ def lib():
         L.ref_set_target_anisotropy.argtypes = [dp, C.c_int]
         L.ref_set_target_anisotropy.restype = None
         L.ref_sst_fields.argtypes = [vp, dp, C.c_int, C.c_double] + [dp] * 12
+        L.ref_observe.argtypes = [vp, C.c_int, C.c_void_p, C.c_double, C.POINTER(State), dp, dp]
         L.ref_linear_solve.argtypes = [C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, dp, dp, C.c_int,
                                        C.c_double, dp]
         L.ref_matvec.argtypes = [C.c_int, C.c_int, ip, ip, dp, dp, dp, dp, dp]
@@ -177,6 +178,31 @@ class RefMesh:
             raise RuntimeError(lib().ref_last_error().decode())
         arrays["turb_established"] = st.turb_established
         return arrays, hist, res
+
+    def observe(self, observables, nu: float, state: dict):
+        """The reference ObservationOperator on `state` (arrays U, p, k, omega,
+        nuT and the boundary values): predictions and the log-likelihood.
+        `observables` is a ctypes array of btm_observable records."""
+        n = len(observables)
+        keep = []
+
+        def arr(a):
+            a = np.ascontiguousarray(a, np.float64).reshape(-1)
+            keep.append(a)
+            return _d(a)
+
+        st = State()
+        st.U, st.Ub = arr(state["U"]), arr(state["Ub"])
+        st.p, st.pb = arr(state["p"]), arr(state["pb"])
+        st.k, st.kb = arr(state["k"]), arr(state["kb"])
+        st.omega, st.omegab = arr(state["omega"]), arr(state["omegab"])
+        st.nuT = arr(state["nuT"])
+        pred = np.zeros(max(n, 1))
+        ll = np.zeros(1)
+        if lib().ref_observe(self.h, n, C.cast(observables, C.c_void_p), float(nu), C.byref(st), _d(pred),
+                             _d(ll)) != 0:
+            raise RuntimeError(lib().ref_last_error().decode())
+        return pred[:n].tolist(), float(ll[0])
 
     def green_gauss(self, phi, phib):
         nC = phi.size

@@ -259,3 +259,37 @@ def write_polymesh_block(path, nx, ny, nz, perturb=0.15, seed=3):
     body += ")\n"
     write("boundary", "polyBoundaryMesh", body)
     return path
+
+
+def bfs_operator():
+    """All six observable kinds on the backward-facing step (recirculating,
+    so separation and reattachment crossings exist; the step face has none)."""
+    from rans_sst_py import ObservationOperator, Vec3
+    o = ObservationOperator()
+    o.add_drag("bottom_wall_down", 0.01, 0.002, 1.0, 1.0)
+    o.add_pressure_tap(Vec3(6.0, 0.5, 0.0), -0.05, 0.01, 1.0)
+    o.add_pressure_tap(Vec3(2.0, 1.5, 0.0), 0.02, 0.01, 1.0, 0.001, 0.1, 1.2)
+    o.add_velocity_profile(Vec3(3.0, 0.3, 0.0), 0, -0.1, 0.05)
+    o.add_velocity_profile(Vec3(3.0, 0.3, 0.0), 1, 0.0, 0.05, 0.01)
+    o.add_skin_friction("bottom_wall_down", Vec3(10.0, 0.0, 0.0), 0.002, 5e-4, 1.0)
+    o.add_skin_friction("top_wall", Vec3(12.0, 3.0, 0.0), 0.003, 5e-4, 1.0)
+    o.add_separation_point("bottom_wall_down", 0.5, 0.1)
+    o.add_reattachment_length("bottom_wall_down", 6.0, 0.5)
+    o.add_reattachment_length("step_face", 0.0, 0.5)
+    return o
+
+
+def channel_operator():
+    """Channel outputs: skin friction on both walls, streamwise velocity at
+    five wall distances, a pressure tap, the wall drag, and a separation
+    point that does not exist (attached flow: the reference's default)."""
+    from rans_sst_py import ObservationOperator, Vec3
+    o = ObservationOperator()
+    o.add_skin_friction("bottom_wall", Vec3(0.5, 0.0, 0.5), 0.0066, 0.001, 1.0)
+    o.add_skin_friction("top_wall", Vec3(0.5, 2.0, 0.5), 0.0066, 0.001, 1.0)
+    for y, u in ((0.001, 0.5), (0.01, 5.0), (0.1, 14.0), (0.5, 19.0), (1.0, 21.0)):
+        o.add_velocity_profile(Vec3(0.5, y, 0.5), 0, u, 0.5)
+    o.add_pressure_tap(Vec3(0.5, 1.0, 0.5), 0.0, 0.01, 20.0)
+    o.add_drag("bottom_wall", 0.0, 0.001, 1.0, 20.0)
+    o.add_separation_point("bottom_wall", 0.5, 0.1)
+    return o

@@ -6,6 +6,8 @@ reference sources exist:
     make -C oracle ref
     python tests/golden/make_golden.py [case ...]
     python tests/golden/make_golden.py bfs_perm_1920+cont   # add the continuation run
+    python tests/golden/make_golden.py bfs_perm_1920+stag   # add the stagnation run
+    python tests/golden/make_golden.py bfs_perm_1920+startup   # add the 3000-iteration start-up
 
 Each .npz holds the exact mesh (MSH1 bytes), the case inputs (nu, settings as
 JSON, initial state) and the reference outputs.  Stagnation states are the
@@ -139,6 +141,44 @@ def add_bfs_continuation():
     a, info, res = ref_solve(bytes(g["mesh"]), m, bcs, nu, s, dict(warm=warm), residual_capacity=200)
     pack("cont200", a, info, g)
     g["cont200_residuals"] = res[:info["iterations_run"]]
+    return g
+
+
+def _bfs_golden_inputs():
+    path = os.path.join(HERE, "bfs_perm_1920.npz")
+    g = dict(np.load(path))
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    m.compute_wall_distance()
+    init = dict(u=tuple(g["init"][:3]), p=float(g["init"][3]), k=float(g["init"][4]), omega=float(g["init"][5]))
+    from rans_sst_py import FlowBoundaryConditions
+    bcs = FlowBoundaryConditions.bfs_defaults(m, 1.0, init["k"], init["omega"])
+    return g, m, bcs, float(g["nu"]), init
+
+
+def add_bfs_startup(iters=3000):
+    """Extend bfs_perm_1920.npz with the reference's cold start run for
+    `iters` outer iterations (convergence test off): its trajectory through
+    the laminar start-up and the switch-on of the turbulence model, the part
+    of the solve that is sensitive to the pressure solver's smoother."""
+    g, m, bcs, nu, init = _bfs_golden_inputs()
+    s = cases.bfs_settings(iters, 0.0)
+    a, info, res = ref_solve(bytes(g["mesh"]), m, bcs, nu, s, init, residual_capacity=iters)
+    pack(f"pin{iters}", a, info, g)
+    g[f"pin{iters}_residuals"] = res[:info["iterations_run"]]
+    return g
+
+
+def add_bfs_stagnation(iters=40000):
+    """Extend bfs_perm_1920.npz with the reference continued from its converged
+    state for `iters` outer iterations with the convergence test off: its
+    stagnation state, the comparator for a device solve continued the same
+    way from its own converged state."""
+    g, m, bcs, nu, init = _bfs_golden_inputs()
+    s = cases.bfs_settings(iters, 0.0)
+    warm = {f: g[f"conv_{f}"] for f in FIELDS}
+    warm["turb_established"] = int(g["conv_turb_established"])
+    a, info, _ = ref_solve(bytes(g["mesh"]), m, bcs, nu, s, dict(warm=warm))
+    pack("stag", a, info, g)
     return g
 
 
@@ -280,11 +320,39 @@ def make_foam_blocks():
     return out
 
 
+def make_observe():
+    """The reference ObservationOperator (core/include/ObservationOperator.hpp:
+    186-378) evaluated by the reference itself on reference states: the
+    converged permuted backward-facing step (cases.bfs_operator: all six
+    kinds) and the stagnated 4x128 Re_tau 550 channel (cases.channel_operator).
+    Requires bfs_perm_1920.npz and c1_chan550_4x128.npz."""
+    from rans_sst_py._lib import observable_structs
+    out = {}
+    for tag, name, prefix, op in (("bfs", "bfs_perm_1920", "conv", cases.bfs_operator()),
+                                  ("chan", "c1_chan550_4x128", "stag", cases.channel_operator())):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        m = cases.mesh_from_bytes(bytes(g["mesh"]))
+        path = "/tmp/_golden_mesh.msh"
+        with open(path, "wb") as fh:
+            fh.write(bytes(g["mesh"]))
+        rm = rd.RefMesh.load(path)
+        rm.wall_distance()
+        arr, n = observable_structs(m, op)
+        state = {f: g[f"{prefix}_{f}"] for f in ("U", "Ub", "p", "pb", "k", "kb", "omega", "omegab", "nuT")}
+        pred, ll = rm.observe(arr, float(g["nu"]), state)
+        out[f"{tag}_pred"] = np.array(pred)
+        out[f"{tag}_loglik"] = np.array(ll)
+        out[f"{tag}_source"] = np.frombuffer(f"{name}:{prefix}".encode(), np.uint8)
+    return out
+
+
 MAKERS = {"units": make_units, "foam_blocks": make_foam_blocks, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
           "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1,
-          "chan180_inject_4x32": make_chan180_inject, "chan180_wallfn_4x32": make_chan180_wallfn}
+          "chan180_inject_4x32": make_chan180_inject, "chan180_wallfn_4x32": make_chan180_wallfn,
+          "observe": make_observe}
 # makers that extend an existing file instead of producing a new case
-EXTENDERS = {"bfs_perm_1920": add_bfs_continuation}
+EXTENDERS = {"bfs_perm_1920+cont": add_bfs_continuation, "bfs_perm_1920+stag": add_bfs_stagnation,
+             "bfs_perm_1920+startup": add_bfs_startup}
 
 
 def main(names):
@@ -292,9 +360,9 @@ def main(names):
         raise SystemExit("reference driver not built: make -C oracle ref")
     for name in names or list(MAKERS):
         t0 = time.time()
-        if name.endswith("+cont"):
-            name = name[:-5]
+        if name in EXTENDERS:
             out = EXTENDERS[name]()
+            name = name.split("+")[0]
         else:
             out = MAKERS[name]()
         path = os.path.join(HERE, name + ".npz")

@@ -70,6 +70,19 @@ def test_mixed_converged_matches_fp64_reference(name):
     _check(errors(out.state, g, "stag"))
 
 
+def test_mixed_c1_stagnation():
+    """The benchmarked mesh (4x128, ratio 1.08, Re_tau 550) in mixed precision,
+    run to the reference's stagnation iteration count: the fixed point agrees
+    with the reference's stagnated FP64 fields within 1e-6."""
+    g = cases.load_golden("c1_chan550_4x128")
+    m = mesh_from(g)
+    bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    case = Case(m, bcs, float(g["nu"]), settings_from(g, 0.0, int(g["stag_iterations_run"])))
+    out = solve(case, COEFF, 0, init_from(g))
+    assert out.iterations_run == int(g["stag_iterations_run"])
+    _check(errors(out.state, g, "stag"))
+
+
 def test_mixed_duct3d_stagnation():
     """3-D duct (z-momentum active), fixed iteration count as the golden."""
     g = cases.load_golden("duct_4x16x16")

@@ -154,3 +154,36 @@ def test_grid_mode_observables():
                        text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert json.loads(r.stdout.strip().splitlines()[-1]) == {"fp64": True, "mixed": True}
+
+
+STATE_FIELDS = ("U", "p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw", "Ub", "pb", "kb", "omegab")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("tag,name,prefix,make", [("bfs", "bfs_perm_1920", "conv", cases.bfs_operator),
+                                                  ("chan", "c1_chan550_4x128", "stag", cases.channel_operator)])
+def test_device_operator_matches_reference(precision, tag, name, prefix, make):
+    """The device evaluation (a zero-iteration warm solve, so the final state
+    is the reference's state) against the predictions and log-likelihood the
+    reference's own ObservationOperator computed (tests/golden/observe.npz):
+    bit-identical."""
+    gold = cases.load_golden("observe")
+    g = cases.load_golden(name)
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    m.compute_wall_distance()
+    a = g["init"]
+    if tag == "bfs":
+        bcs = FlowBoundaryConditions.bfs_defaults(m, 1.0, float(a[4]), float(a[5]))
+        s = cases.bfs_settings(0, 0.0)
+    else:
+        bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+        s = cases.channel_settings(0, 0.0)
+    s.precision = precision
+    case = Case(m, bcs, float(g["nu"]), s)
+    case.set_observations(make())
+    warm = {f: np.array(g[f"{prefix}_{f}"]) for f in STATE_FIELDS}
+    warm["turb_established"] = int(g[f"{prefix}_turb_established"])
+    out = solve(case, cases.COEFF_DEFAULTS, 0, warm, want_state=False)
+    assert out.iterations_run == 0
+    assert np.array_equal(np.array(out.predictions), gold[f"{tag}_pred"]), (out.predictions, gold[f"{tag}_pred"])
+    assert out.log_lik == float(gold[f"{tag}_loglik"])

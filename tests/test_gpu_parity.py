@@ -191,6 +191,8 @@ def _assert_fields(out, g, prefix, tol):
 @pytest.mark.parametrize("name,bcs_fn", [
     ("chan180_4x32", lambda m: FlowBoundaryConditions.channel_defaults(m, 0, 0, 0)),
     ("couette_4x32", lambda m: FlowBoundaryConditions.periodic_couette(m, 40.0)),
+    # the benchmarked mesh: 4x128, ratio 1.08, Re_tau 550 (60000 iterations)
+    ("c1_chan550_4x128", lambda m: FlowBoundaryConditions.channel_defaults(m, 0, 0, 0)),
 ])
 def test_stagnation_parity(name, bcs_fn):
     """Run to the same stagnation iteration count as the reference: 1e-8 rel L2."""

@@ -1,0 +1,221 @@
+"""The reference-order AMG on the device (amg_order = "reference", the
+default of the FP64 engine on unstructured / renumbered meshes) against the
+oracle's restatement of AMGSolver (core/include/LinearSolver.hpp:407-656,
+pinned bit-exact to the reference by tests/test_oracle_pin.py) and the
+reference's own runs (tests/golden/bfs_perm_1920.npz).
+
+Tolerances:
+  * hierarchy built on the device from a pressure-correction matrix: level
+    sizes, aggregation maps, coarse sparsity and coarse values bit-identical
+    to buildAggregates / galerkinProduct;
+  * AMG-preconditioned CG: the same iteration count as the reference, the
+    solution within 1e-12 relative (parallel dot products, reciprocal
+    diagonals in the smoother);
+  * the permuted 1920-cell backward-facing step from the cold start through
+    its laminar start-up and the switch-on of the turbulence model (3000
+    outer iterations, where the multicolour form of the AMG diverges): U, k,
+    omega, nu_t, p within 1e-6 relative L2 of the reference's own state at
+    the same iteration;
+  * the full cold start (opt-in, BTM_LONG_GPU_TESTS=1, about 80k outer
+    iterations): converged within 1 % of the reference's iteration count,
+    then run on to stagnation, U, k, omega, nu_t, p within 1e-8 of the
+    reference's stagnation state and the reattachment length within 1e-8.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from rans_sst_py import Case, FlowBoundaryConditions, ObservationOperator, Vec3, solve
+from test_gpu_parity import COEFF, _dbg, _pack, _rand_state, init_from, mesh_from, settings_from
+
+pytestmark = pytest.mark.gpu
+
+
+def _ldu_to_csr(nC, own, nbr, diag, upper, lower):
+    """lduToCSR (LinearSolver.hpp:344-404): diagonal first, then the faces in
+    ascending order, rows stably sorted by column."""
+    rows = [[(i, diag[i])] for i in range(nC)]
+    for f in range(len(own)):
+        rows[own[f]].append((int(nbr[f]), upper[f]))
+        rows[nbr[f]].append((int(own[f]), lower[f]))
+    rp, col, val = [0], [], []
+    for r in rows:
+        r = sorted(r, key=lambda t: t[0])
+        col += [c for c, _ in r]
+        val += [v for _, v in r]
+        rp.append(len(col))
+    return np.array(rp), np.array(col), np.array(val)
+
+
+def _galerkin(rp, col, val, mp, nc):
+    """galerkinProduct (LinearSolver.hpp:446-485): each coarse entry sums its
+    fine entries in (fine row, fine column) order starting from 0.0."""
+    rows = [dict() for _ in range(nc)]
+    for i in range(len(rp) - 1):
+        I = mp[i]
+        for j in range(rp[i], rp[i + 1]):
+            J = mp[col[j]]
+            rows[I][J] = rows[I].get(J, 0.0) + val[j]
+    rp2, c2, v2 = [0], [], []
+    for r in rows:
+        for J in sorted(r):
+            c2.append(J)
+            v2.append(r[J])
+        rp2.append(len(c2))
+    return np.array(rp2), np.array(c2), np.array(v2)
+
+
+def _device_hierarchy(case, m, st, sysp):
+    nC = m.n_cells()
+    o = _dbg(case, "amg_levels", _pack(m, st, sysp), 64 * nC + 4096)
+    nl = int(o[0])
+    sizes = [int(v) for v in o[1:1 + nl]]
+    at = 22
+    maps = []
+    for l in range(nl - 1):
+        maps.append(o[at:at + sizes[l]].astype(np.int64))
+        at += sizes[l]
+    csr = []
+    for l in range(1, nl):
+        ptr = o[at:at + sizes[l] + 1].astype(np.int64)
+        at += sizes[l] + 1
+        nnz = int(ptr[-1])
+        col = o[at:at + nnz].astype(np.int64)
+        at += nnz
+        val = o[at:at + nnz].copy()
+        at += nnz
+        csr.append((ptr, col, val))
+    return sizes, maps, csr
+
+
+def _cases():
+    m, bcs, nu, _ = cases.bfs_case()
+    yield "bfs_perm_1920", m, bcs, nu, cases.bfs_settings(10, 0.0), True
+    m, _, nu, _ = cases.duct_case(4, 12, 12)
+    m = m.permuted(np.random.default_rng(17).permutation(m.n_cells()))
+    m.compute_wall_distance()
+    bcs = FlowBoundaryConditions.channel_defaults(m, 0.0, 0.0, 0.0)
+    yield "duct_perm_576", m, bcs, nu, cases.channel_settings(10, 0.0), False
+    m, bcs, nu, _ = cases.periodic_channel(32, 180.0)      # grid order: deep wavefronts
+    yield "channel_4x32", m, bcs, nu, cases.channel_settings(10, 0.0), True
+
+
+@pytest.fixture(scope="module", params=list(_cases()), ids=lambda p: p[0])
+def ref_case(request):
+    name, m, bcs, nu, s, zz = request.param
+    s.amg_order = "reference"
+    return name, m, bcs, nu, s, zz, Case(m, bcs, nu, s)
+
+
+def _pressure_system(oracle, m, bcs, nu, s, st):
+    pr = oracle.assemble(m, bcs, nu, s, COEFF, 3, st, aP=st["aP"])
+    return dict(diag=pr["diag"], upper=pr["upper"], lower=pr["lower"], source=pr["source"], x=np.zeros(m.n_cells()))
+
+
+def test_hierarchy_bit_identical(ref_case, oracle):
+    name, m, bcs, nu, s, zz, case = ref_case
+    st = _rand_state(m, np.random.default_rng(31), zz)
+    sysp = _pressure_system(oracle, m, bcs, nu, s, st)
+    nC, nIF = m.n_cells(), m.n_internal_faces()
+    rp, col, val = _ldu_to_csr(nC, m.owner[:nIF], m.neighbour[:nIF], sysp["diag"], sysp["upper"], sysp["lower"])
+    sizes_ref, maps_ref = oracle.amg_levels(rp, col, val)
+    sizes, maps, csr = _device_hierarchy(case, m, st, sysp)
+    assert sizes == sizes_ref and len(sizes) >= 3
+    for l, (a, b) in enumerate(zip(maps, maps_ref)):
+        assert np.array_equal(a, b), f"aggregation map of level {l}"
+    # coarse matrices: the Galerkin product level by level, bit for bit
+    frp, fcol, fval = rp, col, val
+    for l in range(1, len(sizes)):
+        grp, gcol, gval = _galerkin(frp, fcol, fval, maps_ref[l - 1], sizes[l])
+        ptr, ccol, cval = csr[l - 1]
+        assert np.array_equal(ptr, grp) and np.array_equal(ccol, gcol), f"coarse sparsity of level {l}"
+        assert np.array_equal(cval, gval), f"coarse values of level {l}"
+        frp, fcol, fval = grp, gcol, gval
+
+
+def test_amg_pcg_same_iterations(ref_case, oracle):
+    name, m, bcs, nu, s, zz, case = ref_case
+    st = _rand_state(m, np.random.default_rng(32), zz)
+    sysp = _pressure_system(oracle, m, bcs, nu, s, st)
+    nC, nIF = m.n_cells(), m.n_internal_faces()
+    o = _dbg(case, "amgpcg", _pack(m, st, sysp), nC + 4)
+    xr, rr = oracle.linear_solve(3, m.owner[:nIF], m.neighbour[:nIF], sysp["diag"], sysp["upper"], sysp["lower"],
+                                 sysp["source"], np.zeros(nC), s.inner_iterations, s.inner_tolerance)
+    assert int(o[nC]) == int(rr[0]) and int(o[nC + 3]) == int(rr[3])
+    assert abs(o[nC + 2] - rr[2]) <= 1e-12 * rr[2]
+    assert np.max(np.abs(o[:nC] - xr)) <= 1e-12 * np.max(np.abs(xr))
+
+
+def test_auto_order_picks_reference_on_permuted_mesh(oracle):
+    """auto: the BFS (random numbering, 11 wavefronts) solves exactly as with
+    amg_order = reference; the grid-ordered channel (35 wavefronts) as with
+    multicolour."""
+    for mk, expect in ((lambda: cases.bfs_case()[:3], True), (lambda: cases.periodic_channel(32, 180.0)[:3], False)):
+        m, bcs, nu = mk()
+        st = _rand_state(m, np.random.default_rng(33), True)
+        s = cases.bfs_settings(10, 0.0)
+        sysp = _pressure_system(oracle, m, bcs, nu, s, st)
+        nC = m.n_cells()
+        outs = {}
+        for order in ("auto", "reference", "multicolour"):
+            s.amg_order = order
+            outs[order] = _dbg(Case(m, bcs, nu, s), "amgpcg", _pack(m, st, sysp), nC + 4)
+        assert np.array_equal(outs["auto"], outs["reference"]) == expect
+        assert np.array_equal(outs["auto"], outs["multicolour"]) == (not expect)
+
+
+def _bfs_case_from_golden(g, iters, tol):
+    m = mesh_from(g)
+    s = settings_from(g)
+    s.max_iterations, s.convergence_tol, s.precision = iters, tol, "fp64"
+    init = init_from(g)
+    bcs = FlowBoundaryConditions.bfs_defaults(m, 1.0, init["k"], init["omega"])
+    return m, bcs, float(g["nu"]), s, init
+
+
+def test_bfs_startup_follows_reference():
+    g = cases.load_golden("bfs_perm_1920")
+    if "pin3000_U" not in g:
+        pytest.skip("BFS golden has no start-up state")
+    m, bcs, nu, s, init = _bfs_case_from_golden(g, 3000, 0.0)
+    out = solve(Case(m, bcs, nu, s), COEFF, 0, init)
+    assert out.iterations_run == 3000 and not out.diverged
+    errs = {f: cases.rel_l2(out.state[f], g[f"pin3000_{f}"]) for f in ("U", "k", "omega", "nuT", "p")}
+    print("bfs start-up, relative L2 vs the reference at iteration 3000:", errs)
+    for f, e in errs.items():
+        assert e <= 1e-6, (f, e)
+
+
+@pytest.mark.skipif(os.environ.get("BTM_LONG_GPU_TESTS") != "1",
+                    reason="about 80k FP64 outer iterations on one CTA (~15 min); BTM_LONG_GPU_TESTS=1 runs it")
+def test_bfs_cold_start_converges_to_reference_state():
+    g = cases.load_golden("bfs_perm_1920")
+    if "stag_U" not in g:
+        pytest.skip("BFS golden has no stagnation state")
+    n_ref = int(g["conv_iterations_run"])
+    m, bcs, nu, s, init = _bfs_case_from_golden(g, 2 * n_ref, 1e-8)
+    case = Case(m, bcs, nu, s)
+    op = ObservationOperator()
+    op.add_reattachment_length("bottom_wall_down", 6.0, 0.5)
+    op.add_skin_friction("bottom_wall_down", Vec3(10.0, 0.0, 0.0), 0.002, 5e-4, 1.0)
+    case.set_observations(op)
+    out = solve(case, COEFF, 0, init)
+    assert out.converged and not out.diverged
+    assert abs(out.iterations_run - n_ref) <= 0.01 * n_ref, (out.iterations_run, n_ref)
+    conv_err = {f: cases.rel_l2(out.state[f], g[f"conv_{f}"]) for f in ("U", "k", "omega", "nuT", "p")}
+    # on to stagnation from the converged state, as the reference golden
+    s2 = s.copy()
+    s2.max_iterations, s2.convergence_tol = int(g["stag_iterations_run"]), 0.0
+    case2 = Case(m, bcs, nu, s2)
+    case2.set_observations(op)
+    stag = solve(case2, COEFF, 0, out.state)
+    stag_err = {f: cases.rel_l2(stag.state[f], g[f"stag_{f}"]) for f in ("U", "k", "omega", "nuT", "p")}
+    ref_pred = op.evaluate(m, {f: g[f"stag_{f}"] for f in ("U", "p", "k", "omega", "nuT", "Ub", "pb", "kb",
+                                                           "omegab")}, nu)
+    print("bfs cold start:", out.iterations_run, "iterations (reference", n_ref, ") conv err", conv_err,
+          "stagnation err", stag_err, "x_r", stag.predictions[0], "reference x_r", ref_pred[0])
+    for f, e in stag_err.items():
+        assert e <= 1e-8, (f, e)
+    assert abs(stag.predictions[0] - ref_pred[0]) <= 1e-8 * ref_pred[0]
