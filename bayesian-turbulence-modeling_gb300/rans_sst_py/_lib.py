@@ -317,7 +317,7 @@ class Case:
         arr, n = observable_structs(mesh, obs_op)
         ms, keep = mesh_struct(mesh)
         check(self._L.btm_case_set_observations(self.h, C.byref(ms), n, arr))
-        self.n_obs = len(items)
+        self.n_obs = n
 
     def set_target_anisotropy(self, b6):
         """Reynolds-stress injection target, (n_cells*6,) xx yy zz xy xz yz
