@@ -1136,6 +1136,16 @@ constexpr double kStallGain = 0.9;     // ... does not push its best residual be
 // thousands of iterations early.
 constexpr double kStallCeiling = 1e-4;
 constexpr int kAmgRefresh = 8;         // outer iterations between coarse-hierarchy refreshes
+// Delivery rule.  The reference's test (largest scaled residual below the
+// tolerance) stops a solve at a distance from the FP64 fixed point that is
+// proportional to the tolerance: at 1e-8 about 5e-6 (U) and 8e-6 (k) in
+// relative L2 on the 4x128 channel, in the FP64 drop-in and this engine
+// alike.  A mixed solve declares convergence once the test also passes at a
+// tenth of the tolerance (a tenth of that distance), or kDeliverWindow
+// iterations after it first passed at the tolerance when the residual has
+// settled on its floor before reaching the tenth.
+constexpr double kDeliverFraction = 0.1;
+constexpr int kDeliverWindow = 4000;
 
 template <class T>
 __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
@@ -1156,6 +1166,8 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     const int gradAll = I.solveZ ? 7 : 3;
     bool polish = false;
     int polishStart = -1;
+    int passStart = -1;        // first iteration that passed the reference's test in stage 2
+    bool passedNow = false;    // this iteration passed it
     int amgAge = 0;
     double bestRes = INFINITY, winBest = INFINITY;
     int winStart = 0;
@@ -1408,10 +1420,14 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
             !isfinite(eW) || !isfinite(lastKChange) || !isfinite(lastOmChange))
             maxRes = INFINITY;
         const bool settled = !turbScheduled || (turbActive && turbEst);
-        if (polish && maxRes < S.convTol && iter > 0 && settled) {
-            converged = 1;
-            finalIter = iter;
-            break;
+        passedNow = polish && maxRes < S.convTol && iter > 0 && settled;
+        if (passedNow) {
+            if (passStart < 0) passStart = iter;
+            if (maxRes < kDeliverFraction * S.convTol || iter - passStart >= kDeliverWindow) {
+                converged = 1;
+                finalIter = iter;
+                break;
+            }
         }
         if (isnan(maxRes) || isinf(maxRes) || maxRes > S.divLimit) {
             diverged = 1;
@@ -1442,6 +1458,12 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
                 polishStart = iter + 1;
             }
         }
+    }
+    if (!converged && !diverged && passedNow) {
+        // the iteration cap ended the delivery window: the reference's own
+        // test passed on the last iteration
+        converged = 1;
+        finalIter = ran - 1;
     }
     tm.sync();
     if (!polish) {

@@ -18,8 +18,10 @@ from ._forward import ForwardModel, SolveOutput, solve, solve_batch
 from ._lib import Case, BtmError, library_path
 from ._server import Server
 from ._sensitivity import ParameterSensitivity, TangentGradientResult
+from ._outputs import cf_along_wall, channel_profile
 
 __all__ = ["Mesh", "BCType", "EvaluationResult", "EvaluationStatus", "FlowBoundaryConditions",
            "InferenceParameterSet", "PatchBC", "SolverSettings", "SSTCoefficients", "Vec3",
            "ObservationOperator", "ForwardModel", "SolveOutput", "solve", "solve_batch", "Case",
-           "BtmError", "library_path", "Server", "ParameterSensitivity", "TangentGradientResult"]
+           "BtmError", "library_path", "Server", "ParameterSensitivity", "TangentGradientResult",
+           "cf_along_wall", "channel_profile"]

@@ -346,10 +346,30 @@ def make_observe():
     return out
 
 
+def make_outputs():
+    """The reference's own wall diagnostics (python/wall_diagnostics.py:77-100,
+    cf_along_wall, imported from the reference sources) on the stagnated 4x128
+    Re_tau 550 channel, both walls, reference velocities 1 and 20."""
+    ref_py = os.path.join(os.environ.get("BTM_REFERENCE_ROOT", "/root/reference"), "python")
+    sys.path.insert(0, ref_py)
+    import wall_diagnostics as wd
+    g = np.load(os.path.join(HERE, "c1_chan550_4x128.npz"))
+    m = cases.mesh_from_bytes(bytes(g["mesh"]))
+    st = {f: g[f"stag_{f}"] for f in ("U", "p", "k", "omega", "nuT")}
+    out = {}
+    for wall in ("bottom_wall", "top_wall"):
+        for uref in (1.0, 20.0):
+            r = wd.cf_along_wall(m, st, float(g["nu"]), wall, uref)
+            for key in ("x", "y", "cf"):
+                out[f"{wall}_{uref:g}_{key}"] = np.asarray(r[key])
+            out[f"{wall}_{uref:g}_mean"] = np.array(r["mean"])
+    return out
+
+
 MAKERS = {"units": make_units, "foam_blocks": make_foam_blocks, "chan180_4x32": make_chan180, "bfs_perm_1920": make_bfs,
           "couette_4x32": make_couette, "duct_4x16x16": make_duct, "c1_chan550_4x128": make_c1,
           "chan180_inject_4x32": make_chan180_inject, "chan180_wallfn_4x32": make_chan180_wallfn,
-          "observe": make_observe}
+          "observe": make_observe, "outputs": make_outputs}
 # makers that extend an existing file instead of producing a new case
 EXTENDERS = {"bfs_perm_1920+cont": add_bfs_continuation, "bfs_perm_1920+stag": add_bfs_stagnation,
              "bfs_perm_1920+startup": add_bfs_startup}
