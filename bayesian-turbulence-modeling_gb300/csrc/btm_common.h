@@ -17,6 +17,9 @@ constexpr int kCoarseDirect = 32;    // coarsest level at or below this size: de
 constexpr int kCoarseDirectGrid = 1024;
 constexpr int kCoarseSweeps = 50;    // GS sweeps when the coarsest level is larger
 constexpr int kRedSlots = 4;         // values per fused team reduction
+// Meshes numbered with at most this bandwidth (max |owner - neighbour|) solve
+// the mixed engine's pressure correction by a banded Cholesky factorisation
+constexpr int kBandMax = 8;
 
 // Boundary-condition codes per boundary face (resolved on the host from the
 // per-patch btm_patch_bc list in patch order, last patch wins).
@@ -146,6 +149,7 @@ struct DevMesh {
     // lower-index neighbours)
     const int32_t *r0Ent;
     int32_t nnz0, nWf0;
+    int32_t band;          // bandwidth of the cell numbering when <= kBandMax on a one-CTA mesh, else 0
     const int32_t *wf0Off, *wf0Rows;
     DevGeom32 g32;
     ObsDev obs;
@@ -181,6 +185,8 @@ struct DevWork32 {
     float *r, *rh, *pv, *v, *s, *t, *ph, *sh, *rd, *x;
     float *amgVal, *amgX, *amgB, *amgR, *amgRd;
     double *ainv, *gj;     // FP64 dense inverse of the coarsest level and its Gauss-Jordan buffers
+    float *band;           // [nC * (2 kBandMax + 1)] banded Cholesky factor of the pressure correction
+    float *bandRd;         // [nC] reciprocal diagonal of that factor
     double *mflux;         // [nIF] FP64 face mass flux (convective defect, continuity defect)
     double *src64;         // [nC] FP64 pressure-correction right-hand side (refinement)
 };
@@ -257,7 +263,7 @@ int engine_launch_debug(DevInst *dInst, void *stream);
 int engine_wall_distance(const double *dCentres, int nC, const double *dWall, int nW, double *dOut, void *stream);
 
 // mixed-precision engine entry points (btm_mixed.cu)
-size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN);
+size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN, int band);
 int mixed_launch_block(DevInst *dInsts, int n, int threads, size_t smemBytes, void *stream);
 int mixed_grid_blocks(int *blocks_out);
 int mixed_launch_grid(DevInst *dInst, int blocks, void *stream);

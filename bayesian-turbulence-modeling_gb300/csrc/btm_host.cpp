@@ -586,6 +586,13 @@ void build_case(btm_case *C, const btm_mesh *m, const btm_patch_bc *bcs, std::ve
         D.nWf0 = nWf;
         D.nnz0 = (int32_t)L0.colIdx.size();
     }
+    // bandwidth of the cell numbering (banded pressure-correction solve of the
+    // mixed engine on one-CTA meshes)
+    {
+        int bw = 0;
+        for (int f = 0; f < nIF; ++f) bw = std::max(bw, std::abs(own[f] - nbr[f]));
+        D.band = (!gridMesh && bw > 0 && bw <= btm::kBandMax) ? bw : 0;
+    }
     D.nLevels = nL;
     D.coarseDirect = lv.back().n <= directMax ? 1 : 0;
     C->amgCoarseN = lv.back().n;
@@ -790,6 +797,7 @@ void ensure_mixed(btm_case *C, Slab &S) {
     floats += up(std::max<int64_t>(C->amgValTotal, 1)) + 3 * up(std::max<int64_t>(C->amgVecTotal, 1)) +
               up((size_t)nC + C->amgVecTotal) + up((size_t)2 * nc * nc) + up((size_t)8 * nc * nc);
     floats += 2 * face + 2 * cell;            // FP64 mass flux [nIF] and right-hand side [nC]
+    floats += up((size_t)nC * (2 * btm::kBandMax + 1)) + cell;   // banded Cholesky factor (two layouts), 1 / diagonal
     const size_t bytes = floats * 4 + 512;
     char *base = nullptr;
     ck(cudaMalloc((void **)&base, bytes), "cudaMalloc(instance fp32)");
@@ -819,6 +827,8 @@ void ensure_mixed(btm_case *C, Slab &S) {
     F.gj = (double *)take((size_t)8 * nc * nc);
     F.mflux = (double *)take(2 * (size_t)std::max(nIF, 1));
     F.src64 = (double *)take(2 * (size_t)nC);
+    F.band = take((size_t)nC * (2 * btm::kBandMax + 1));
+    F.bandRd = take(nC);
     if ((size_t)((char *)d - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "fp32 slab overflow");
 }
 
@@ -1477,7 +1487,7 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                     const btm_case *Cm = jobs[i].C;
                     maxCells = std::max(maxCells, Cm->nC);
                     smem = std::max(smem, btm::mixed_smem_bytes(Cm->nC, Cm->nIF, Cm->amgVecTotal, Cm->amgValTotal,
-                                                                Cm->dmesh.coarseDirect ? Cm->amgCoarseN : 1));
+                                                                Cm->dmesh.coarseDirect ? Cm->amgCoarseN : 1, Cm->dmesh.band));
                 }
                 int e = btm::mixed_launch_block(dInsts + blockIdx.size(), (int)mixIdx.size(),
                                                 block_threads_for(maxCells), smem, st);

@@ -1023,6 +1023,180 @@ __device__ __noinline__ SolveResF mx_pcg(T &tm, const DevMesh &M, DevWork32 &F, 
 }
 
 // makeSolver semantics: AMG and PCG run the CG family, every other name BiCGSTAB
+// ---- banded Cholesky for the pressure correction ----------------------------
+// On a mesh numbered with a small bandwidth b (a channel b cells wide
+// numbered across the span first: b = 4 on the 4 x n_y channels) the SPD
+// correction matrix is factored A = L L^T in its band once per outer
+// iteration and every correction solve (the first and the FP64-defect
+// refinement passes) is two substitutions.  This replaces the AMG-PCG loop,
+// whose V-cycle is ~30 dependent CTA-wide phases per iteration on these
+// meshes; the correction then meets the inner tolerance after one FP64
+// refinement pass (FP32 factor of a matrix with condition ~1e5).  The
+// pressure correction vanishes at convergence, so the fixed point does not
+// depend on how it is solved.
+//
+// Layout (F.band, n (2 kBandMax + 1) floats): the lower band of A, column k
+// at band[k (b+1) + d] = A[k+d][k] (d = 0..b), factored in place into L; and
+// a row-major copy of L's off-diagonal part, row k at band[n (b+1) + k b + t]
+// = L[k][k-b+t], so a substitution step reads one contiguous row.
+//
+// The factor runs on one thread with the latest b columns of L in registers
+// (W[t][d] = L[j+d][j] for j = k-b+t): each column costs a chain of b fused
+// multiply-adds and a reciprocal square root, and its loads do not wait on
+// that chain.  The substitutions keep the last b values in registers.
+template <int B>
+__device__ bool band_factor_1t(float *band, float *rd, int n) {
+    constexpr int w = B + 1;
+    float *Lr = band + (size_t)n * w;
+    float W[B][B + 1];
+#pragma unroll
+    for (int t = 0; t < B; ++t)
+#pragma unroll
+        for (int d = 0; d <= B; ++d) W[t][d] = 0.0f;
+    bool ok = true;
+#pragma unroll 4
+    for (int k = 0; k < n; ++k) {
+        float col[B + 1];
+#pragma unroll
+        for (int d = 0; d <= B; ++d) col[d] = (k + d < n) ? band[(size_t)k * w + d] : 0.0f;
+        // col[d] = A[k+d][k] - sum_j L[k+d][j] L[k][j], j = k-B+t with d <= t
+#pragma unroll
+        for (int d = 0; d <= B; ++d)
+#pragma unroll
+            for (int t = 0; t < B; ++t)
+                if (d <= t) col[d] = fmaf(-W[t][B - t + d], W[t][B - t], col[d]);
+        const float piv = col[0];
+        ok = ok && piv > 0.0f && piv < INFINITY;
+        const float rl = rsqrtf(piv);
+        float nc[B + 1];
+        nc[0] = piv * rl;
+#pragma unroll
+        for (int d = 1; d <= B; ++d) nc[d] = col[d] * rl;
+#pragma unroll
+        for (int d = 0; d <= B; ++d) band[(size_t)k * w + d] = nc[d];
+        rd[k] = rl;
+        // row-major copy: L[k+d][k] is entry t = B - d of row k+d
+#pragma unroll
+        for (int d = 1; d <= B; ++d)
+            if (k + d < n) Lr[(size_t)(k + d) * B + (B - d)] = nc[d];
+#pragma unroll
+        for (int t = 0; t + 1 < B; ++t)
+#pragma unroll
+            for (int d = 0; d <= B; ++d) W[t][d] = W[t + 1][d];
+#pragma unroll
+        for (int d = 0; d <= B; ++d) W[B - 1][d] = nc[d];
+    }
+    // rows 0..B-1 have entries before column 0: zero them (read as L = 0)
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+#pragma unroll
+        for (int t = 0; t < B; ++t)
+            if (k < n && k - B + t < 0) Lr[(size_t)k * B + t] = 0.0f;
+    return ok;
+}
+
+template <int B>
+__device__ void band_solve_1t(const float *band, const float *rd, const float *src, float scale, float *x, int n) {
+    constexpr int w = B + 1;
+    const float *Lr = band + (size_t)n * w;
+    // forward: y_k = (scale src_k - sum_t L[k][k-B+t] y_{k-B+t}) / L[k][k]; win[t] = y_{k-B+t}
+    float win[B];
+#pragma unroll
+    for (int t = 0; t < B; ++t) win[t] = 0.0f;
+#pragma unroll 4
+    for (int k = 0; k < n; ++k) {
+        float l[B];
+#pragma unroll
+        for (int t = 0; t < B; ++t) l[t] = Lr[(size_t)k * B + t];
+        float s = src[k] * scale;
+#pragma unroll
+        for (int t = 0; t < B; ++t) s = fmaf(-l[t], win[t], s);
+        const float y = s * rd[k];
+        x[k] = y;
+#pragma unroll
+        for (int t = 0; t + 1 < B; ++t) win[t] = win[t + 1];
+        win[B - 1] = y;
+    }
+    // backward: x_k = (y_k - sum_d L[k+d][k] x_{k+d}) / L[k][k]; win[d-1] = x_{k+d}
+#pragma unroll
+    for (int t = 0; t < B; ++t) win[t] = 0.0f;
+#pragma unroll 4
+    for (int k = n - 1; k >= 0; --k) {
+        float l[B];
+#pragma unroll
+        for (int d = 1; d <= B; ++d) l[d - 1] = band[(size_t)k * w + d];
+        float s = x[k];
+#pragma unroll
+        for (int d = B; d >= 1; --d) s = fmaf(-l[d - 1], win[d - 1], s);
+        const float xk = s * rd[k];
+        x[k] = xk;
+#pragma unroll
+        for (int t = B - 1; t > 0; --t) win[t] = win[t - 1];
+        win[0] = xk;
+    }
+}
+
+// Gathers the lower band of the FP32 correction matrix per row (duplicate
+// faces summed in face order), then factors it on one thread.  Returns false
+// on every thread when a pivot is not positive (the caller falls back to the
+// AMG-PCG solve).
+template <class T>
+__device__ __noinline__ bool mx_band_factor(T &tm, const DevMesh &M, DevWork32 &F) {
+    __shared__ int okFlag;
+    const int n = M.nC, b = M.band, w = b + 1;
+    float *Lb = F.band;
+    for (int q = tm.rank(); q < n * w; q += tm.size()) Lb[q] = 0.0f;
+    tm.sync();
+    for (int i = tm.rank(); i < n; i += tm.size()) {
+        Lb[(size_t)i * w] = LD(F.diag + i);
+        for (int e = M.cfOff[i]; e < M.cfOff[i + 1]; ++e) {
+            const int f = M.cfFace[e], oth = M.cfOther[e];
+            const int c = oth >= 0 ? oth : -(oth + 1);
+            if (c >= i) continue;
+            // row i's entry for column c: upper when i owns the face, lower when it is the neighbour
+            Lb[(size_t)c * w + (i - c)] += oth >= 0 ? LD(F.upper + f) : LD(F.lower + f);
+        }
+    }
+    tm.sync();
+    if (tm.rank() == 0) {
+        bool ok = false;
+        switch (b) {
+            case 1: ok = band_factor_1t<1>(Lb, F.bandRd, n); break;
+            case 2: ok = band_factor_1t<2>(Lb, F.bandRd, n); break;
+            case 3: ok = band_factor_1t<3>(Lb, F.bandRd, n); break;
+            case 4: ok = band_factor_1t<4>(Lb, F.bandRd, n); break;
+            case 5: ok = band_factor_1t<5>(Lb, F.bandRd, n); break;
+            case 6: ok = band_factor_1t<6>(Lb, F.bandRd, n); break;
+            case 7: ok = band_factor_1t<7>(Lb, F.bandRd, n); break;
+            case 8: ok = band_factor_1t<8>(Lb, F.bandRd, n); break;
+        }
+        okFlag = ok ? 1 : 0;
+    }
+    tm.sync();
+    return okFlag != 0;
+}
+
+// x = A^{-1} (scale * src) with the band factor: forward L y = scale src,
+// backward L^T x = y, on one thread.
+template <class T>
+__device__ __noinline__ SolveResF mx_band_solve(T &tm, const DevMesh &M, DevWork32 &F, float *x, float scale) {
+    if (tm.rank() == 0) {
+        const int n = M.nC;
+        switch (M.band) {
+            case 1: band_solve_1t<1>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 2: band_solve_1t<2>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 3: band_solve_1t<3>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 4: band_solve_1t<4>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 5: band_solve_1t<5>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 6: band_solve_1t<6>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 7: band_solve_1t<7>(F.band, F.bandRd, F.src, scale, x, n); break;
+            case 8: band_solve_1t<8>(F.band, F.bandRd, F.src, scale, x, n); break;
+        }
+    }
+    tm.sync();
+    return SolveResF{1, 0.0f, 1};
+}
+
 template <class T>
 __device__ SolveResF mx_solve(T &tm, const DevMesh &M, DevWork32 &F, int kind, float *x, float scale, int maxIter,
                               float tol, bool amgSetup) {
@@ -1141,11 +1315,11 @@ constexpr int kAmgRefresh = 8;         // outer iterations between coarse-hierar
 // proportional to the tolerance: at 1e-8 about 5e-6 (U) and 8e-6 (k) in
 // relative L2 on the 4x128 channel, in the FP64 drop-in and this engine
 // alike.  A mixed solve declares convergence once the test also passes at a
-// tenth of the tolerance (a tenth of that distance), or kDeliverWindow
-// iterations after it first passed at the tolerance when the residual has
-// settled on its floor before reaching the tenth.
+// tenth of the tolerance (a tenth of that distance), or, when the residual
+// settles on its floor above that tenth, once kDeliverWindow iterations
+// after the first pass have not lowered its best value by 10 %.
 constexpr double kDeliverFraction = 0.1;
-constexpr int kDeliverWindow = 4000;
+constexpr int kDeliverWindow = 2000;
 
 template <class T>
 __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
@@ -1166,8 +1340,9 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     const int gradAll = I.solveZ ? 7 : 3;
     bool polish = false;
     int polishStart = -1;
-    int passStart = -1;        // first iteration that passed the reference's test in stage 2
-    bool passedNow = false;    // this iteration passed it
+    int passStart = -1;        // last iteration that lowered the best passing residual by 10 %
+    double passBest = INFINITY;
+    bool passedNow = false;    // this iteration passed the reference's test in stage 2
     int amgAge = 0;
     double bestRes = INFINITY, winBest = INFINITY;
     int winStart = 0;
@@ -1261,13 +1436,20 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         clk.lap(3);
         if (eP > 0.0) {
             const double s = 1.0 / eP;
-            if (S.pSolver == 3) {
+            bool band = M.band > 0 && (S.pSolver == 3 || S.pSolver == 0);
+            if (band) {
+                band = mx_band_factor(tm, M, F);
+                if (!band) amgAge = 0;   // the AMG fallback starts from a fresh hierarchy
+                clk.lap(4);
+            }
+            if (!band && S.pSolver == 3) {
                 // a hierarchy shared with AMG solves of other systems is rebuilt every time
                 mx_amg_setup(tm, M, F, amgAge == 0 || S.momSolver == 3 || S.turbSolver == 3);
                 amgAge = amgAge + 1 == kAmgRefresh ? 0 : amgAge + 1;
                 clk.lap(4);
             }
-            const SolveResF rp = mx_solve(tm, M, F, S.pSolver, F.pp, (float)s, S.innerIter, innerTol, false);
+            const SolveResF rp = band ? mx_band_solve(tm, M, F, F.pp, (float)s)
+                                      : mx_solve(tm, M, F, S.pSolver, F.pp, (float)s, S.innerIter, innerTol, false);
             innerP += rp.iterations;
             tm.sync();
             for (int pass = 0; pass < kMaxRefine; ++pass) {
@@ -1275,8 +1457,9 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
                 tm.template sumd<1>(dd);
                 const double dn = sqrt(dd[0]);
                 if (!(dn > S.innerTol)) break;
-                const SolveResF rq = mx_solve(tm, M, F, S.pSolver, F.x, (float)(1.0 / dn), S.innerIter,
-                                              (float)(S.innerTol / dn), false);
+                const SolveResF rq = band ? mx_band_solve(tm, M, F, F.x, (float)(1.0 / dn))
+                                          : mx_solve(tm, M, F, S.pSolver, F.x, (float)(1.0 / dn), S.innerIter,
+                                                     (float)(S.innerTol / dn), false);
                 innerRef += rq.iterations;
                 tm.sync();
                 for (int c = tm.rank(); c < nC; c += tm.size()) F.pp[c] = fmaf(F.x[c], (float)dn, F.pp[c]);
@@ -1422,7 +1605,10 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         const bool settled = !turbScheduled || (turbActive && turbEst);
         passedNow = polish && maxRes < S.convTol && iter > 0 && settled;
         if (passedNow) {
-            if (passStart < 0) passStart = iter;
+            if (maxRes < 0.9 * passBest) {
+                passBest = maxRes;
+                passStart = iter;
+            }
             if (maxRes < kDeliverFraction * S.convTol || iter - passStart >= kDeliverWindow) {
                 converged = 1;
                 finalIter = iter;
@@ -1524,20 +1710,32 @@ struct SmemCopy {
 
 __device__ __host__ inline size_t smem_round(size_t b) { return (b + kSmemAlign - 1) & ~size_t(kSmemAlign - 1); }
 
-// sizes in placement order (bytes); returns the count
-__device__ __host__ inline int smem_items(int nC, int nIF, int64_t vec, int64_t val, int nc, int nGather, size_t *sz) {
-    int q = 0;
-    sz[q++] = 4 * ((size_t)nC + 2 * (size_t)nIF);                  // diag | upper | lower
-    for (int i = 0; i < 7; ++i) sz[q++] = 4 * (size_t)nC;           // r s t pv v pp x
-    sz[q++] = 4 * ((size_t)nC + (size_t)vec);                       // amgRd
-    for (int i = 0; i < 3; ++i) sz[q++] = 4 * (size_t)(vec > 0 ? vec : 1);   // amgX amgB amgR
-    sz[q++] = 4 * (size_t)(val > 0 ? val : 1);                      // amgVal
-    for (int i = 0; i < 5; ++i) sz[q++] = 4 * (size_t)nC;           // rh ph sh rd src
-    sz[q++] = 8 * (size_t)nc * nc;                                  // coarse inverse (FP64)
-    sz[q++] = 4 * ((size_t)nC + 1);                                 // cfOff
-    sz[q++] = 4 * (size_t)nGather;                                  // cfFace
-    sz[q++] = 4 * (size_t)nGather;                                  // cfOther
-    return q;
+// Staged arrays in placement order (the hottest first); an array that does
+// not fit, or that the instance does not use, stays in global memory.
+enum SmemItem : int {
+    SI_SYS = 0, SI_BAND, SI_BANDRD, SI_R, SI_S, SI_T, SI_PV, SI_V, SI_PP, SI_X, SI_AMGRD, SI_AMGX, SI_AMGB, SI_AMGR,
+    SI_AMGVAL, SI_RH, SI_PH, SI_SH, SI_RD, SI_SRC, SI_AINV, SI_CFOFF, SI_CFFACE, SI_CFOTHER, SI_COUNT
+};
+
+// sizes in placement order (bytes, 0: not staged); returns the count.  With
+// a band factor (band > 0) the pressure correction does not use the AMG
+// arrays, which stay in global memory for the fallback solve.
+__device__ __host__ inline int smem_items(int nC, int nIF, int64_t vec, int64_t val, int nc, int nGather, int band,
+                                          size_t *sz) {
+    const bool amg = band == 0;
+    sz[SI_SYS] = 4 * ((size_t)nC + 2 * (size_t)nIF);                  // diag | upper | lower
+    sz[SI_BAND] = band ? 4 * (size_t)nC * (2 * band + 1) : 0;          // banded Cholesky factor, two layouts
+    sz[SI_BANDRD] = band ? 4 * (size_t)nC : 0;
+    for (int q = SI_R; q <= SI_X; ++q) sz[q] = 4 * (size_t)nC;         // r s t pv v pp x
+    sz[SI_AMGRD] = amg ? 4 * ((size_t)nC + (size_t)vec) : 0;
+    for (int q = SI_AMGX; q <= SI_AMGR; ++q) sz[q] = amg ? 4 * (size_t)(vec > 0 ? vec : 1) : 0;
+    sz[SI_AMGVAL] = amg ? 4 * (size_t)(val > 0 ? val : 1) : 0;
+    for (int q = SI_RH; q <= SI_SRC; ++q) sz[q] = 4 * (size_t)nC;      // rh ph sh rd src
+    sz[SI_AINV] = amg ? 8 * (size_t)nc * nc : 0;                       // coarse inverse (FP64)
+    sz[SI_CFOFF] = 4 * ((size_t)nC + 1);
+    sz[SI_CFFACE] = 4 * (size_t)nGather;
+    sz[SI_CFOTHER] = 4 * (size_t)nGather;
+    return SI_COUNT;
 }
 
 __device__ void stage_smem(DevMesh &M, DevInst &I, unsigned char *dsm, size_t cap, SmemCopy *copies, int *nCopies) {
@@ -1545,39 +1743,41 @@ __device__ void stage_smem(DevMesh &M, DevInst &I, unsigned char *dsm, size_t ca
     const int nC = M.nC, nIF = M.nIF;
     const int nc = M.coarseDirect ? M.lev[M.nLevels - 1].n : 1;
     const int nGather = 2 * nIF;
-    size_t sz[32];
-    const int nItems = smem_items(nC, nIF, M.amgVecTotal, M.amgValTotal, nc, nGather, sz);
+    size_t sz[SI_COUNT];
+    const int nItems = smem_items(nC, nIF, M.amgVecTotal, M.amgValTotal, nc, nGather, M.band, sz);
     size_t off = 0;
     int nc_ = 0;
     for (int q = 0; q < nItems; ++q) {
         const size_t b = smem_round(sz[q]);
-        if (off + b > cap) continue;
+        if (b == 0 || off + b > cap) continue;
         void *p = dsm + off;
         off += b;
         float *f = (float *)p;
         switch (q) {
-            case 0: F.diag = f; F.upper = f + nC; F.lower = f + nC + nIF; break;
-            case 1: F.r = f; break;
-            case 2: F.s = f; break;
-            case 3: F.t = f; break;
-            case 4: F.pv = f; break;
-            case 5: F.v = f; break;
-            case 6: F.pp = f; break;
-            case 7: F.x = f; break;
-            case 8: F.amgRd = f; break;
-            case 9: F.amgX = f; break;
-            case 10: F.amgB = f; break;
-            case 11: F.amgR = f; break;
-            case 12: F.amgVal = f; break;
-            case 13: F.rh = f; break;
-            case 14: F.ph = f; break;
-            case 15: F.sh = f; break;
-            case 16: F.rd = f; break;
-            case 17: F.src = f; break;
-            case 18: F.ainv = (double *)p; break;
-            case 19: copies[nc_++] = {p, M.cfOff, (int)sz[q]}; M.cfOff = (const int32_t *)p; break;
-            case 20: copies[nc_++] = {p, M.cfFace, (int)sz[q]}; M.cfFace = (const int32_t *)p; break;
-            case 21: copies[nc_++] = {p, M.cfOther, (int)sz[q]}; M.cfOther = (const int32_t *)p; break;
+            case SI_SYS: F.diag = f; F.upper = f + nC; F.lower = f + nC + nIF; break;
+            case SI_BAND: F.band = f; break;
+            case SI_BANDRD: F.bandRd = f; break;
+            case SI_R: F.r = f; break;
+            case SI_S: F.s = f; break;
+            case SI_T: F.t = f; break;
+            case SI_PV: F.pv = f; break;
+            case SI_V: F.v = f; break;
+            case SI_PP: F.pp = f; break;
+            case SI_X: F.x = f; break;
+            case SI_AMGRD: F.amgRd = f; break;
+            case SI_AMGX: F.amgX = f; break;
+            case SI_AMGB: F.amgB = f; break;
+            case SI_AMGR: F.amgR = f; break;
+            case SI_AMGVAL: F.amgVal = f; break;
+            case SI_RH: F.rh = f; break;
+            case SI_PH: F.ph = f; break;
+            case SI_SH: F.sh = f; break;
+            case SI_RD: F.rd = f; break;
+            case SI_SRC: F.src = f; break;
+            case SI_AINV: F.ainv = (double *)p; break;
+            case SI_CFOFF: copies[nc_++] = {p, M.cfOff, (int)sz[q]}; M.cfOff = (const int32_t *)p; break;
+            case SI_CFFACE: copies[nc_++] = {p, M.cfFace, (int)sz[q]}; M.cfFace = (const int32_t *)p; break;
+            case SI_CFOTHER: copies[nc_++] = {p, M.cfOther, (int)sz[q]}; M.cfOther = (const int32_t *)p; break;
         }
     }
     *nCopies = nc_;
@@ -1647,9 +1847,9 @@ int mixed_launch_grid(DevInst *dInst, int blocks, void *stream) {
 }
 
 // dynamic shared memory that would hold an instance's whole solver working set
-size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN) {
-    size_t sz[32];
-    const int n = smem_items(nC, nIF, vecTotal, valTotal, coarseN, 2 * nIF, sz);
+size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int coarseN, int band) {
+    size_t sz[SI_COUNT];
+    const int n = smem_items(nC, nIF, vecTotal, valTotal, coarseN, 2 * nIF, band, sz);
     size_t t = 0;
     for (int q = 0; q < n; ++q) t += smem_round(sz[q]);
     return t;

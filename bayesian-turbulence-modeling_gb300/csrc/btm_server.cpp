@@ -145,7 +145,7 @@ void dispatch(btm_server *S) {
             refAmg = refAmg || s->slab.inst.S.refAmg;
             if (s->mixed)
                 smem = std::max(smem, btm::mixed_smem_bytes(s->C->nC, s->C->nIF, s->C->amgVecTotal, s->C->amgValTotal,
-                                                             s->C->dmesh.coarseDirect ? s->C->amgCoarseN : 1));
+                                                             s->C->dmesh.coarseDirect ? s->C->amgCoarseN : 1, s->C->dmesh.band));
         }
         // requests that wait on a warm-start tag: their copies were issued on
         // the copy stream, which this launch orders after

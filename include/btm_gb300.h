@@ -81,9 +81,9 @@ extern "C" {
  * state, equation defects, continuity defect and pressure-correction
  * refinement, and an FP64-assembly final stage, so a converged solve
  * satisfies the FP64 discrete equations.  A mixed solve is converged when
- * the reference's test passes at a tenth of convergence_tol (or 4000
- * iterations after it first passed at convergence_tol, if the residual
- * settles before that): the reference's test at a tolerance t stops a solve
+ * the reference's test passes at a tenth of convergence_tol (or, passing at
+ * convergence_tol, when 2000 iterations have not lowered the residual by
+ * 10 %: its floor): the reference's test at a tolerance t stops a solve
  * a distance proportional to t from the fixed point (about 8e-6 relative L2
  * at t = 1e-8 on the 4x128 channel), so a converged mixed solve lies within
  * a tenth of that.  No reference counterpart. */
