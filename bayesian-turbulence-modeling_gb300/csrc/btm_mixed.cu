@@ -1310,6 +1310,10 @@ constexpr double kStallGain = 0.9;     // ... does not push its best residual be
 // thousands of iterations early.
 constexpr double kStallCeiling = 1e-4;
 constexpr int kAmgRefresh = 8;         // outer iterations between coarse-hierarchy refreshes
+// Outer iterations between band factorisations: the factor of a recent
+// correction matrix solves the current one within the FP64-defect
+// refinement passes that follow every correction solve.
+constexpr int kBandRefresh = 4;
 // Delivery rule.  The reference's test (largest scaled residual below the
 // tolerance) stops a solve at a distance from the FP64 fixed point that is
 // proportional to the tolerance: at 1e-8 about 5e-6 (U) and 8e-6 (k) in
@@ -1344,6 +1348,8 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     double passBest = INFINITY;
     bool passedNow = false;    // this iteration passed the reference's test in stage 2
     int amgAge = 0;
+    int bandAge = 0;           // outer iterations since the band factor was formed
+    bool bandOk = true;        // the last band factorisation succeeded
     double bestRes = INFINITY, winBest = INFINITY;
     int winStart = 0;
     PhaseClock clk;
@@ -1436,12 +1442,13 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         clk.lap(3);
         if (eP > 0.0) {
             const double s = 1.0 / eP;
-            bool band = M.band > 0 && (S.pSolver == 3 || S.pSolver == 0);
-            if (band) {
-                band = mx_band_factor(tm, M, F);
+            bool band = M.band > 0 && (S.pSolver == 3 || S.pSolver == 0) && bandOk;
+            if (band && bandAge == 0) {
+                band = bandOk = mx_band_factor(tm, M, F);
                 if (!band) amgAge = 0;   // the AMG fallback starts from a fresh hierarchy
                 clk.lap(4);
             }
+            if (band) bandAge = bandAge + 1 == kBandRefresh ? 0 : bandAge + 1;
             if (!band && S.pSolver == 3) {
                 // a hierarchy shared with AMG solves of other systems is rebuilt every time
                 mx_amg_setup(tm, M, F, amgAge == 0 || S.momSolver == 3 || S.turbSolver == 3);
