@@ -510,13 +510,66 @@ __device__ __noinline__ SolveResult team_pcg(T &tm, const DevMesh &M, DevInst &I
     return res;
 }
 
-// makeSolver semantics for the device: AMG and PCG run the CG family; every
-// other name runs BiCGSTAB.  Gauss-Seidel is not offered on the device (the
-// host rejects it at case creation).
+// GaussSeidelSolver::solve (LinearSolver.hpp:258-299) on (I.diag, I.upper,
+// I.lower, I.src), x in place: in-place sweeps in row order, each row summing
+// its neighbours in face order with the latest values, then a residual check
+// against |source|.  A sweep runs wavefront by wavefront over the level-0
+// row-order dependencies (M.wf0Off / M.wf0Rows): a row reads the new values
+// of its lower-index neighbours and the old values of the others, exactly as
+// the sequential sweep, with the reference's operation order per row.  Only
+// the residual norm (a parallel reduction) differs in the last bits.
+template <class T>
+__device__ __noinline__ SolveResult team_gauss_seidel(T &tm, const DevMesh &M, DevInst &I, double *x, int maxIter,
+                                                      double tol) {
+    SolveResult res = {0, 0.0, 0.0, 0};
+    const int nC = M.nC;
+    double a0[1] = {0.0};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const double bc = LD(I.src + c);
+        a0[0] = fma(bc, bc, a0[0]);
+    }
+    tm.template sum<1>(a0);
+    double b0 = sqrt(a0[0]);
+    res.initialRes = b0;
+    if (b0 < 1e-30) b0 = 1.0;
+    for (int it = 0; it < maxIter; ++it) {
+        if (!tm.ok()) break;
+        for (int w = 0; w < M.nWf0; ++w) {
+            for (int q = M.wf0Off[w] + tm.rank(); q < M.wf0Off[w + 1]; q += tm.size()) {
+                const int i = M.wf0Rows[q];
+                const double d = LD(I.diag + i);
+                if (fabs(d) <= 1e-30) continue;
+                double sacc = LD(I.src + i);
+                for (int e = M.cfOff[i]; e < M.cfOff[i + 1]; ++e) {
+                    const int f = M.cfFace[e], oth = M.cfOther[e];
+                    if (oth >= 0) sacc -= LD(I.upper + f) * LD(x + oth);
+                    else sacc -= LD(I.lower + f) * LD(x + (-(oth + 1)));
+                }
+                x[i] = sacc / d;
+            }
+            tm.sync();
+        }
+        double a1[1] = {0.0};
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const double rc = LD(I.src + c) - ldu_row<T>(M, I, x, c);
+            a1[0] = fma(rc, rc, a1[0]);
+        }
+        tm.template sum<1>(a1);
+        res.iterations = it + 1;
+        res.finalRes = sqrt(a1[0]) / b0;
+        if (res.finalRes < tol) { res.converged = 1; return res; }
+    }
+    return res;
+}
+
+// makeSolver semantics for the device (LinearSolver.hpp:659-665): AMG and
+// PCG run the CG family, GaussSeidel the in-place sweep; every other name
+// runs BiCGSTAB.
 template <class T>
 __device__ SolveResult team_solve(T &tm, const DevMesh &M, DevInst &I, int kind, double *x, int maxIter, double tol) {
     if (kind == 3) return team_amg_pcg(tm, M, I, x, maxIter, tol);
     if (kind == 0) return team_pcg(tm, M, I, x, maxIter, tol);
+    if (kind == 2) return team_gauss_seidel(tm, M, I, x, maxIter, tol);
     return team_bicgstab(tm, M, I, x, maxIter, tol);
 }
 
@@ -894,6 +947,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_debug(DevInst *inst) {
             break;
         case 11:  // PCG (Jacobi)
             res = team_pcg(tm, M, I, I.pp, I.S.innerIter, I.S.innerTol);
+            break;
+        case 13:  // Gauss-Seidel
+            res = team_gauss_seidel(tm, M, I, I.pp, I.S.innerIter, I.S.innerTol);
             break;
         case 12:  // reference-order AMG hierarchy of (diag, upper, lower)
             if (I.S.refAmg) res.iterations = ramg_setup(tm, M, I);

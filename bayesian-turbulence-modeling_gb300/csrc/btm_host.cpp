@@ -335,8 +335,8 @@ btm::DevSettings dev_settings(const btm_settings &s) {
 void check_settings(const btm_settings &s) {
     if (s.turb_update_interval <= 0) throw BtmError(BTM_ERR_ARG, "turb_update_interval must be positive");
     for (int code : {s.pressure_solver, s.momentum_solver, s.turbulence_solver}) {
-        if (code == BTM_LS_GAUSSSEIDEL)
-            throw BtmError(BTM_ERR_ARG, "the GaussSeidel linear solver is not available on the device");
+        if (code == BTM_LS_GAUSSSEIDEL && s.precision == BTM_PREC_MIXED)
+            throw BtmError(BTM_ERR_ARG, "the GaussSeidel linear solver runs in the FP64 engine only");
         if (code < 0 || code > 3) throw BtmError(BTM_ERR_ARG, "unknown linear solver code");
     }
     if (!(s.alpha_u > 0) || !(s.alpha_k > 0) || !(s.alpha_omega > 0))
@@ -1046,6 +1046,94 @@ int block_threads_for(int maxCells) {
     return maxCells <= small ? 256 : 512;
 }
 
+// ---- launch-shape autotuner ---------------------------------------------------
+// A case that runs one CTA per instance (block mode) can launch 256-thread
+// CTAs (two per SM with the engines' 128 registers per thread) or 512-thread
+// CTAs (one per SM).  On its first solve the tuner times both on a probe
+// batch of up to two instances per SM (cold starts of the case with the
+// request's coefficients, kTuneIters outer iterations, convergence test off,
+// on slabs allocated for the probe and freed after it) and keeps the faster
+// for the case and engine.  The choice belongs to the case, not to a batch,
+// so an instance's reductions (and its result bits) are the same alone and
+// in any batch.  BTM_BLOCK_THREADS=256|512 forces a shape, BTM_AUTOTUNE=0
+// keeps the size rule (256 threads up to BTM_SMALL_CELLS cells).
+constexpr int kTuneIters = 40;
+constexpr size_t kTuneBytes = size_t(512) << 20;   // device memory the probe slabs may take
+
+int case_threads(const btm_case *C, int engine) {
+    static int forced = env_int("BTM_BLOCK_THREADS", 0);
+    if (forced == 256 || forced == 512) return forced;
+    if (C->tunedThreads[engine] > 0) return C->tunedThreads[engine];
+    return block_threads_for(C->nC);
+}
+
+void autotune_case(btm_case *C, const double *coeffs, int variant) {
+    static int enabled = env_int("BTM_AUTOTUNE", 1);
+    const int engine = C->settings.precision == BTM_PREC_MIXED ? 1 : 0;
+    if (!enabled || C->tunedThreads[engine] != 0 || C->nC > block_max_cells() || C->dmesh.bTarget) return;
+    int dev = 0, sms = 1;
+    ck(cudaGetDevice(&dev), "device");
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    std::vector<Slab> probe(1);
+    make_slab(C, probe[0]);
+    if (engine == 1) ensure_mixed(C, probe[0]);
+    const size_t per = probe[0].bytes + probe[0].bytes32;
+    const int nProbe = (int)std::max<size_t>(1, std::min<size_t>(2 * (size_t)sms, kTuneBytes / std::max<size_t>(per, 1)));
+    cudaStream_t st = C->stream;
+    btm::DevInst *d = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    auto release = [&]() {
+        cudaStreamSynchronize(st);
+        for (Slab &S : probe) free_slab(S);
+        if (d) cudaFree(d);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    };
+    try {
+        probe.resize(nProbe);
+        std::vector<btm::DevInst> arr;
+        bool refAmg = false;
+        for (int q = 0; q < nProbe; ++q) {
+            Slab &S = probe[q];
+            if (!S.dptr) make_slab(C, S);
+            if (engine == 1) ensure_mixed(C, S);
+            fill_inst(C, S.inst, coeffs, variant, nullptr);
+            S.inst.S.maxIter = kTuneIters;
+            S.inst.S.convTol = 0.0;
+            ensure_ramg(C, S);
+            refAmg = refAmg || S.inst.S.refAmg;
+            ck(cudaMemsetAsync(S.inst.barrier, 0, 512, st), "memset control");
+            arr.push_back(S.inst);
+        }
+        ck(cudaMalloc((void **)&d, sizeof(btm::DevInst) * nProbe), "cudaMalloc(tune insts)");
+        ck(cudaMemcpyAsync(d, arr.data(), sizeof(btm::DevInst) * nProbe, cudaMemcpyHostToDevice, st), "tune insts");
+        ck(cudaEventCreate(&ev[0]), "event");
+        ck(cudaEventCreate(&ev[1]), "event");
+        const size_t smem = engine == 1 ? btm::mixed_smem_bytes(C->nC, C->nIF, C->amgVecTotal, C->amgValTotal,
+                                                                C->dmesh.coarseDirect ? C->amgCoarseN : 1, C->dmesh.band)
+                                        : 0;
+        float ms[2] = {0.0f, 0.0f};
+        const int shapes[2] = {256, 512};
+        for (int k = 0; k < 2; ++k) {
+            ck(cudaEventRecord(ev[0], st), "event");
+            const int e = engine == 0 ? btm::engine_launch_block(d, nProbe, shapes[k], st, refAmg, C->nC)
+                                      : btm::mixed_launch_block(d, nProbe, shapes[k], smem, st);
+            if (e) throw BtmError(BTM_ERR_CUDA, std::string("tune launch: ") + cudaGetErrorString((cudaError_t)e));
+            ck(cudaEventRecord(ev[1], st), "event");
+            ck(cudaStreamSynchronize(st), "tune");
+            ck(cudaEventElapsedTime(&ms[k], ev[0], ev[1]), "event time");
+        }
+        C->tuneMs[engine][0] = ms[0];
+        C->tuneMs[engine][1] = ms[1];
+        C->tuneProbe[engine] = nProbe;
+        C->tunedThreads[engine] = ms[1] < ms[0] ? 512 : 256;
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+}
+
 struct Job {
     btm_case *C;
     Slab *S;
@@ -1060,6 +1148,18 @@ struct Job {
 extern "C" {
 
 const char *btm_last_error(void) { return g_err.c_str(); }
+
+int btm_case_launch_shape(const btm_case *c, int32_t precision, int32_t *threads, int32_t *tuned, int32_t *probe,
+                          double *probe_ms) {
+    if (!c || !threads || (precision != BTM_PREC_FP64 && precision != BTM_PREC_MIXED))
+        return fail(BTM_ERR_ARG, "bad argument");
+    const int engine = precision == BTM_PREC_MIXED ? 1 : 0;
+    *threads = c->nC > block_max_cells() ? 0 : case_threads(c, engine);
+    if (tuned) *tuned = c->tunedThreads[engine] > 0 ? 1 : 0;
+    if (probe) *probe = c->tuneProbe[engine];
+    if (probe_ms) { probe_ms[0] = c->tuneMs[engine][0]; probe_ms[1] = c->tuneMs[engine][1]; }
+    return BTM_OK;
+}
 double btm_last_launch_ms(void) { return g_launch_ms; }
 int btm_abi_version(void) { return BTM_ABI_VERSION; }
 
@@ -1382,6 +1482,9 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
     if (n == 0) return BTM_OK;
     if (int e = ensure_device()) return e;
     try {
+        // first one-CTA solve of a case: choose its launch shape
+        for (int i = 0; i < n; ++i)
+            if (cases[i]) autotune_case(cases[i], coeffs + 11 * (size_t)i, variants ? variants[i] : 0);
         // take per-case slabs (reused across calls)
         std::vector<Job> jobs(n);
         std::vector<int> used;
@@ -1455,43 +1558,51 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                 gridIdx.push_back(i);
             }
         }
-        // one persistent launch per engine for all block-mode instances
+        // one persistent launch per engine and launch shape for all
+        // block-mode instances: an instance runs with its case's shape
+        // (autotuned or by rule), whatever else is in the batch, so its
+        // result is the same bits alone and in any batch
         ck(cudaEventCreate(&res.ev[0]), "event");
         ck(cudaEventCreate(&res.ev[1]), "event");
         cudaEvent_t ev0 = res.ev[0], ev1 = res.ev[1];
         btm::DevInst *dInsts = nullptr;
         const size_t nBlock = blockIdx.size() + mixIdx.size();
         if (nBlock > 0) {
+            struct Group { int engine, threads; std::vector<int> idx; };
+            std::vector<Group> groups;
+            for (int engine = 0; engine < 2; ++engine)
+                for (int threads : {256, 512}) {
+                    Group g{engine, threads, {}};
+                    for (int i : engine == 0 ? blockIdx : mixIdx)
+                        if (case_threads(jobs[i].C, engine) == threads) g.idx.push_back(i);
+                    if (!g.idx.empty()) groups.push_back(std::move(g));
+                }
             std::vector<btm::DevInst> arr;
-            for (int i : blockIdx) arr.push_back(jobs[i].S->inst);
-            for (int i : mixIdx) arr.push_back(jobs[i].S->inst);
+            for (const Group &g : groups)
+                for (int i : g.idx) arr.push_back(jobs[i].S->inst);
             ck(cudaMalloc((void **)&dInsts, sizeof(btm::DevInst) * arr.size()), "cudaMalloc(insts)");
             res.dev.push_back(dInsts);
             ck(cudaMemcpyAsync(dInsts, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
             ck(cudaEventRecord(ev0, st), "event");
-            if (!blockIdx.empty()) {
+            size_t at = 0;
+            for (const Group &g : groups) {
                 int maxCells = 0;
                 bool refAmg = false;
-                for (int i : blockIdx) {
-                    maxCells = std::max(maxCells, jobs[i].C->nC);
-                    refAmg = refAmg || jobs[i].S->inst.S.refAmg;
-                }
-                int e = btm::engine_launch_block(dInsts, (int)blockIdx.size(), block_threads_for(maxCells), st, refAmg,
-                                                 maxCells);
-                if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
-            }
-            if (!mixIdx.empty()) {
-                int maxCells = 0;
                 size_t smem = 0;
-                for (int i : mixIdx) {
+                for (int i : g.idx) {
                     const btm_case *Cm = jobs[i].C;
                     maxCells = std::max(maxCells, Cm->nC);
-                    smem = std::max(smem, btm::mixed_smem_bytes(Cm->nC, Cm->nIF, Cm->amgVecTotal, Cm->amgValTotal,
-                                                                Cm->dmesh.coarseDirect ? Cm->amgCoarseN : 1, Cm->dmesh.band));
+                    refAmg = refAmg || jobs[i].S->inst.S.refAmg;
+                    if (g.engine == 1)
+                        smem = std::max(smem, btm::mixed_smem_bytes(Cm->nC, Cm->nIF, Cm->amgVecTotal, Cm->amgValTotal,
+                                                                    Cm->dmesh.coarseDirect ? Cm->amgCoarseN : 1,
+                                                                    Cm->dmesh.band));
                 }
-                int e = btm::mixed_launch_block(dInsts + blockIdx.size(), (int)mixIdx.size(),
-                                                block_threads_for(maxCells), smem, st);
-                if (e) throw BtmError(BTM_ERR_CUDA, std::string("mixed launch: ") + cudaGetErrorString((cudaError_t)e));
+                const int e = g.engine == 0
+                                  ? btm::engine_launch_block(dInsts + at, (int)g.idx.size(), g.threads, st, refAmg, maxCells)
+                                  : btm::mixed_launch_block(dInsts + at, (int)g.idx.size(), g.threads, smem, st);
+                if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
+                at += g.idx.size();
             }
         } else {
             ck(cudaEventRecord(ev0, st), "event");
@@ -1712,7 +1823,8 @@ int btm_debug_phase(btm_case *C, int32_t phase, const double *coeffs, int32_t va
             case BTM_PHASE_SPMV: srcs = {I.v}; lens = {nC}; break;
             case BTM_PHASE_BICGSTAB:
             case BTM_PHASE_AMGPCG:
-            case BTM_PHASE_PCG: srcs = {I.pp, I.outLast}; lens = {nC, 4}; break;
+            case BTM_PHASE_PCG:
+            case BTM_PHASE_GS: srcs = {I.pp, I.outLast}; lens = {nC, 4}; break;
             default: throw BtmError(BTM_ERR_ARG, "unknown debug phase");
         }
         int64_t total = 0;
@@ -1743,6 +1855,7 @@ void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, 
 }
 int block_max_cells() { return ::block_max_cells(); }
 int block_threads_for(int maxCells) { return ::block_threads_for(maxCells); }
+int case_threads(const btm_case *C, int engine) { return ::case_threads(C, engine); }
 void make_slab(btm_case *C, Slab &S) { ::make_slab(C, S); }
 void ensure_mixed(btm_case *C, Slab &S) { ::ensure_mixed(C, S); }
 void ensure_obs(btm_case *C, Slab &S, bool want) { ::ensure_obs(C, S, want); }

@@ -47,6 +47,12 @@ struct btm_case {
     double injMaxViolation = 0.0;
     std::mutex mtx;
     cudaStream_t stream = nullptr;
+    // launch shape per engine (FP64, mixed): CTA threads chosen by the
+    // autotuner (0: not tuned), its probe size and the probe times (ms) of
+    // 256- and 512-thread CTAs
+    int tunedThreads[2] = {0, 0};
+    int tuneProbe[2] = {0, 0};
+    double tuneMs[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
 };
 
 namespace btm_host {
@@ -59,6 +65,9 @@ void set_launch_ms(double ms);
 void fill_inst(btm_case *C, btm::DevInst &I, const double *coeffs, int variant, const btm_init *init);
 int block_max_cells();
 int block_threads_for(int maxCells);
+// CTA threads of a case's one-CTA launches for engine 0 (FP64) / 1 (mixed):
+// forced, autotuned, or by the size rule
+int case_threads(const btm_case *C, int engine);
 // instance slab (FP64 fields and work) and its FP32 bulk for the mixed engine
 void make_slab(btm_case *C, Slab &S);
 void ensure_mixed(btm_case *C, Slab &S);

@@ -231,7 +231,7 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     if (!ck(cudaMemcpyAsync(dI, &I, sizeof I, cudaMemcpyHostToDevice, st), "instance descriptor"))
         return drain(BTM_ERR_CUDA);
     if (!ck(cudaEventRecord(ev[0], st), "event")) return drain(BTM_ERR_CUDA);
-    int le = btm::engine_launch_block(dI, 1, btm_host::block_threads_for(C->nC), st, refAmg, C->nC);
+    int le = btm::engine_launch_block(dI, 1, btm_host::case_threads(C, 0), st, refAmg, C->nC);
     if (le) {
         btm_host::set_error(std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
         return drain(BTM_ERR_CUDA);

@@ -127,7 +127,7 @@ void dispatch(btm_server *S) {
     std::vector<Slot *> groups[4];   // [engine * 2 + (CTA size 512)]
     for (auto &p : S->slots)
         if (p->state == Slot::PENDING) {
-            const int big = btm_host::block_threads_for(p->C->nC) == 512 ? 1 : 0;
+            const int big = btm_host::case_threads(p->C, p->mixed ? 1 : 0) == 512 ? 1 : 0;
             groups[(p->mixed ? 2 : 0) + big].push_back(p.get());
         }
     for (int g = 0; g < 4; ++g) {
@@ -157,7 +157,7 @@ void dispatch(btm_server *S) {
         btm::DevInst *d = nullptr;
         sck(cudaMallocAsync((void **)&d, sizeof(btm::DevInst) * arr.size(), st), "cudaMallocAsync(insts)");
         sck(cudaMemcpyAsync(d, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
-        const int threads = btm_host::block_threads_for(maxCells);
+        const int threads = (g & 1) ? 512 : 256;
         int e = engine == 0 ? btm::engine_launch_block(d, (int)arr.size(), threads, st, refAmg, maxCells)
                             : btm::mixed_launch_block(d, (int)arr.size(), threads, smem, st);
         if (e) throw SrvError(BTM_ERR_CUDA, std::string("server launch: ") + cudaGetErrorString((cudaError_t)e));

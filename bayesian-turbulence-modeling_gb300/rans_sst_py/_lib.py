@@ -80,7 +80,7 @@ SOLVER_CODES = {"PCG": 0, "BiCGSTAB": 1, "GaussSeidel": 2, "AMG": 3}
 PRECISION_CODES = {"fp64": 0, "mixed": 1}
 AMG_ORDER_CODES = {"auto": 0, "reference": 1, "multicolour": 2}
 PHASES = {"grad": 1, "sst": 2, "momentum": 3, "pressure": 4, "k": 5, "omega": 6, "spmv": 7,
-          "bicgstab": 8, "amgpcg": 9, "pcg": 11, "amg_levels": 12}
+          "bicgstab": 8, "amgpcg": 9, "pcg": 11, "amg_levels": 12, "gs": 13}
 
 _lib = None
 _lock = threading.Lock()
@@ -104,6 +104,8 @@ def lib():
             L.btm_case_destroy.argtypes = [C.c_void_p]
             L.btm_case_destroy.restype = None
             L.btm_case_info.argtypes = [C.c_void_p] + [C.POINTER(C.c_int32)] * 4
+            L.btm_case_launch_shape.argtypes = [C.c_void_p, C.c_int32] + [C.POINTER(C.c_int32)] * 3 + \
+                [C.POINTER(C.c_double)]
             L.btm_case_set_settings.argtypes = [C.c_void_p, C.POINTER(BtmSettings)]
             L.btm_case_set_observations.argtypes = [C.c_void_p, C.POINTER(BtmMesh), C.c_int32,
                                                     C.POINTER(BtmObservable)]
@@ -304,6 +306,16 @@ class Case:
         check(self._L.btm_case_info(self.h, *[C.byref(x) for x in v]))
         return dict(n_cells=v[0].value, n_boundary_faces=v[1].value, n_amg_levels=v[2].value,
                     is_2d=bool(v[3].value))
+
+    def launch_shape(self, precision="fp64"):
+        """The case's one-CTA launch shape in an engine (btm_case_launch_shape):
+        CTA threads, whether the autotuner chose them, its probe size and the
+        probe times of 256- and 512-thread CTAs (ms)."""
+        th, tu, pr = C.c_int32(), C.c_int32(), C.c_int32()
+        ms = (C.c_double * 2)()
+        check(self._L.btm_case_launch_shape(self.h, PRECISION_CODES[precision], C.byref(th), C.byref(tu), C.byref(pr),
+                                            ms))
+        return dict(threads=th.value, tuned=bool(tu.value), probe=pr.value, probe_ms=[ms[0], ms[1]])
 
     def set_settings(self, settings):
         st = settings_struct(settings)

@@ -420,6 +420,7 @@ def run_gpu(args, world, rank, local):
     clk = clocks.summary()
     step_s, e2e_s, converged_all, value, e2e_value = aggregate_ranks(world, dev_ms, wall_s, conv_counts)
     converged = statistics.mean(conv_counts)
+    shape = case.launch_shape(PRECISION)
     h2d = n * (11 * 8 + 4 + 48)
     nb = m.n_boundary_faces()
     d2h = n * 8 * (m.n_cells() * 11 + nb * 6)
@@ -447,6 +448,9 @@ def run_gpu(args, world, rank, local):
                        "iters_per_converged_solve": iters_per_solve,
                        "inner_iters_per_outer": inner / max(1, outer),
                        "polish_start_frac": statistics.mean(polish) if polish else None,
+                       "launch_shape": {"cta_threads": shape["threads"], "autotuned": shape["tuned"],
+                                        "probe_instances": shape["probe"],
+                                        "probe_ms_256_512": shape["probe_ms"]},
                        "l2": "working set L2/shared-memory resident; no flush needed for a single persistent "
                              "launch per step"},
             "latency_ms": {"p50": float(np.percentile(fin, 50)), "p99": float(np.percentile(fin, 99)),

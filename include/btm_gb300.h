@@ -342,6 +342,16 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs,
                     const int32_t *variants, const btm_init *inits,
                     btm_state *outs, btm_history *hists);
 
+/* Launch shape of a case's one-CTA solves in an engine (precision BTM_PREC_*):
+ * CTA threads (256: two instances per SM, 512: one; 0 when the mesh runs on
+ * the cooperative grid), whether the autotuner chose it, and the tuner's
+ * probe (instances) and its times in ms for 256 and 512 threads.  The tuner
+ * runs on the first one-CTA solve of a case in each engine (no reference
+ * counterpart: it replaces the hand-set pool sizes of the calibration
+ * drivers, python/UQ/datasets/channel_calibration.py:189-222). */
+int btm_case_launch_shape(const btm_case *c, int32_t precision, int32_t *threads, int32_t *tuned, int32_t *probe,
+                          double *probe_ms);
+
 /* Device time of the kernel launches made by the most recent solve call on
  * this thread, measured with CUDA events on the launching stream (ms); a
  * profiling hook with no reference counterpart. */
@@ -360,6 +370,7 @@ double btm_last_launch_ms(void);
 #define BTM_PHASE_BICGSTAB      8   /* BiCGSTABSolver::solve                   */
 #define BTM_PHASE_AMGPCG        9   /* AMG-preconditioned CG                   */
 #define BTM_PHASE_PCG          11   /* PCGSolver::solve (Jacobi-preconditioned CG) */
+#define BTM_PHASE_GS           13   /* GaussSeidelSolver::solve                */
 #define BTM_PHASE_AMG_LEVELS   12   /* AMGSolver::setup in the reference order (needs
                                        amg_order = BTM_AMG_REFERENCE): out = level
                                        count, 21 level sizes, the aggregation map of

@@ -283,8 +283,8 @@ def make_chan180_inject():
 def make_chan180_wallfn():
     """Wall functions on (useWallFunctions: eddy viscosity at wall faces in the
     momentum flux, the blended omega wall value, SIMPLESolver.cpp:115, 894-903)
-    on the Re_tau 180 4x32 channel: 50 iterations and 2000 iterations from
-    the cold start."""
+    on the Re_tau 180 4x32 channel: 50, 2000 and 20000 iterations (its
+    stagnation) from the cold start."""
     m, bcs, nu, init = cases.periodic_channel(32, 180.0)
     s = cases.channel_settings(50, 0.0)
     s.use_wall_functions = True
@@ -294,6 +294,9 @@ def make_chan180_wallfn():
     s.max_iterations = 2000
     a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
     pack("pin2000", a, info, out)
+    s.max_iterations = 20000
+    a, info, _ = ref_solve(mb, m, bcs, nu, s, init)
+    pack("stag", a, info, out)
     return out
 
 
