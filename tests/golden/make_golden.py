@@ -353,7 +353,8 @@ def make_outputs():
     """The reference's own wall diagnostics (python/wall_diagnostics.py:77-100,
     cf_along_wall, imported from the reference sources) on the stagnated 4x128
     Re_tau 550 channel, both walls, reference velocities 1 and 20."""
-    ref_py = os.path.join(os.environ.get("BTM_REFERENCE_ROOT", "/root/reference"), "python")
+    ref_root = os.environ.get("BTM_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference")
+    ref_py = os.path.join(ref_root, "python")
     sys.path.insert(0, ref_py)
     import wall_diagnostics as wd
     g = np.load(os.path.join(HERE, "c1_chan550_4x128.npz"))
