@@ -68,12 +68,12 @@ __device__ void phase_bc_w(T &tm, const DevMesh &M, DevInst &I, double beta1, bo
 
 // per-phase device timers, kept by the team leader
 struct PhaseClock {
-    uint64_t acc[8];
+    uint64_t acc[kPhaseSlots];
     uint64_t t0;
     bool on;
     __device__ void start(bool leader) {
         on = leader;
-        for (int q = 0; q < 8; ++q) acc[q] = 0;
+        for (int q = 0; q < kPhaseSlots; ++q) acc[q] = 0;
         t0 = on ? globaltimer_ns() : 0;
     }
     __device__ __forceinline__ void lap(int phase) {

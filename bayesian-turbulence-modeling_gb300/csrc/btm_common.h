@@ -17,6 +17,11 @@ constexpr int kCoarseDirect = 32;    // coarsest level at or below this size: de
 constexpr int kCoarseDirectGrid = 1024;
 constexpr int kCoarseSweeps = 50;    // GS sweeps when the coarsest level is larger
 constexpr int kRedSlots = 4;         // values per fused team reduction
+constexpr int kAndersonMax = 8;      // stored differences of the Anderson acceleration (BTM_ANDERSON_MAX)
+constexpr int kAaFields = 6;         // Ux, Uy, Uz, p, k, omega
+// per-phase device timers: closure, momentum assembly, momentum solve, p' assembly,
+// p' solver setup, p' solve, corrections, turbulence, Anderson update, other
+constexpr int kPhaseSlots = 10;
 // Meshes numbered with at most this bandwidth (max |owner - neighbour|) solve
 // the mixed engine's pressure correction by a banded Cholesky factorisation
 constexpr int kBandMax = 8;
@@ -167,6 +172,7 @@ struct DevSettings {
     double kMin, kMax, omegaMin, vonKarman;
     double alphaInj;       // blend factor of the Reynolds-stress injection source
     int32_t refAmg;        // AMG solves use the reference-order AMG (btm_ramg.cuh)
+    int32_t aaDepth;       // mixed engine: Anderson depth of the outer iteration (0: off)
 };
 
 // FP32 bulk of one mixed-precision instance: closure fields, gradients, the
@@ -189,6 +195,12 @@ struct DevWork32 {
     float *bandRd;         // [nC] reciprocal diagonal of that factor
     double *mflux;         // [nIF] FP64 face mass flux (convective defect, continuity defect)
     double *src64;         // [nC] FP64 pressure-correction right-hand side (refinement)
+    // Anderson acceleration of the outer iteration: vectors over the
+    // interior state, element v*nC + c for field v in (Ux, Uy, Uz, p, k, omega)
+    double *aaX;           // [kAaFields nC] the iterate the current outer iteration started from
+    double *aaGprev;       // [kAaFields nC] the previous outer iteration's result
+    float *aaFprev;        // [kAaFields nC] the previous weighted change (result - iterate)
+    float *aaDF, *aaDG;    // [kAndersonMax][kAaFields nC] differences of successive changes / results
 };
 
 struct DevInst {
@@ -225,7 +237,7 @@ struct DevInst {
     // outputs
     int32_t *out;           // [8]: status, converged, diverged, finalIter, itersRun, turbEst, _, _
     int64_t *outInner;      // [5] inner iterations: total, momentum, pressure, turbulence, refinement
-    uint64_t *outTime;      // [10] ns per phase [0..7] (leader thread's globaltimer), solve start [8] and end [9]
+    uint64_t *outTime;      // [12] ns per phase [0..9] (leader thread's globaltimer), solve start [10] and end [11]
     double *outLast;        // [6] last residual entry, [6..8] the residual scales used
     double *hist;           // [histCap*6] or null
     int32_t histCap;

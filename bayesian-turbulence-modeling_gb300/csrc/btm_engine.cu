@@ -816,9 +816,9 @@ __device__ void simple_solve(T &tm, const DevMesh &M, DevInst &I) {
             clk.acc[5] -= I.rg.setupNs;
             clk.acc[4] += I.rg.setupNs;
         }
-        for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
-        I.outTime[8] = tStart;
-        I.outTime[9] = globaltimer_ns();
+        for (int q = 0; q < kPhaseSlots; ++q) I.outTime[q] = clk.acc[q];
+        I.outTime[kPhaseSlots] = tStart;
+        I.outTime[kPhaseSlots + 1] = globaltimer_ns();
         if (I.obsOut) observe_leader<T>(M, I);
         if (I.doneFlag) {
             __threadfence_system();

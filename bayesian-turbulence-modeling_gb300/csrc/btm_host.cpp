@@ -329,6 +329,7 @@ btm::DevSettings dev_settings(const btm_settings &s) {
     d.omegaMin = s.omega_min;
     d.vonKarman = s.von_karman;
     d.alphaInj = s.alpha_injection;
+    d.aaDepth = s.anderson_depth;
     return d;
 }
 
@@ -345,6 +346,8 @@ void check_settings(const btm_settings &s) {
         throw BtmError(BTM_ERR_ARG, "unknown precision code");
     if (s.amg_order < BTM_AMG_AUTO || s.amg_order > BTM_AMG_MULTICOLOUR)
         throw BtmError(BTM_ERR_ARG, "unknown amg_order code");
+    if (s.anderson_depth < 0 || s.anderson_depth > BTM_ANDERSON_MAX)
+        throw BtmError(BTM_ERR_ARG, "anderson_depth must be in [0, BTM_ANDERSON_MAX]");
 }
 
 // hostOnly: stop after the (validated) host AMG hierarchy and return it
@@ -798,6 +801,8 @@ void ensure_mixed(btm_case *C, Slab &S) {
               up((size_t)nC + C->amgVecTotal) + up((size_t)2 * nc * nc) + up((size_t)8 * nc * nc);
     floats += 2 * face + 2 * cell;            // FP64 mass flux [nIF] and right-hand side [nC]
     floats += up((size_t)nC * (2 * btm::kBandMax + 1)) + cell;   // banded Cholesky factor (two layouts), 1 / diagonal
+    const size_t aaLen = (size_t)btm::kAaFields * nC;             // Anderson vectors
+    floats += 2 * up(2 * aaLen) + up(aaLen) + 2 * up(btm::kAndersonMax * aaLen);
     const size_t bytes = floats * 4 + 512;
     char *base = nullptr;
     ck(cudaMalloc((void **)&base, bytes), "cudaMalloc(instance fp32)");
@@ -829,6 +834,11 @@ void ensure_mixed(btm_case *C, Slab &S) {
     F.src64 = (double *)take(2 * (size_t)nC);
     F.band = take((size_t)nC * (2 * btm::kBandMax + 1));
     F.bandRd = take(nC);
+    F.aaX = (double *)take(2 * aaLen);
+    F.aaGprev = (double *)take(2 * aaLen);
+    F.aaFprev = take(aaLen);
+    F.aaDF = take(btm::kAndersonMax * aaLen);
+    F.aaDG = take(btm::kAndersonMax * aaLen);
     if ((size_t)((char *)d - base) > bytes) throw BtmError(BTM_ERR_INTERNAL, "fp32 slab overflow");
 }
 
@@ -1629,12 +1639,14 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
         if (se == cudaSuccess && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) g_launch_ms = ms;
         if (se != cudaSuccess) throw BtmError(BTM_ERR_CUDA, std::string("solve: ") + cudaGetErrorString(se));
         // per-instance device timestamps: [8] start, [9] end of each solve
-        std::vector<std::array<uint64_t, 10>> times(n);
+        std::vector<std::array<uint64_t, btm::kPhaseSlots + 2>> times(n);
         uint64_t t0 = 0;
         for (int i = 0; i < n; ++i) {
-            ck(cudaMemcpy(times[i].data(), jobs[i].S->inst.outTime, sizeof(uint64_t) * 10, cudaMemcpyDeviceToHost),
+            ck(cudaMemcpy(times[i].data(), jobs[i].S->inst.outTime, sizeof(uint64_t) * (btm::kPhaseSlots + 2),
+                          cudaMemcpyDeviceToHost),
                "status");
-            if (times[i][8] && (!t0 || times[i][8] < t0)) t0 = times[i][8];
+            const uint64_t ts = times[i][btm::kPhaseSlots];
+            if (ts && (!t0 || ts < t0)) t0 = ts;
         }
         for (int i = 0; i < n; ++i) {
             Job &J = jobs[i];
@@ -1661,9 +1673,10 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                 for (int q = 0; q < 4; ++q) h.inner_split[q] = innerv[q + 1];
                 h.polish_start = outv[7];
                 for (int q = 0; q < 6; ++q) h.last_residual[q] = lastv[q];
-                for (int q = 0; q < 8; ++q) h.phase_ms[q] = 1e-6 * (double)tns[q];
-                h.solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
-                h.finish_ms = (t0 && tns[9] > t0) ? 1e-6 * (double)(tns[9] - t0) : 0.0;
+                for (int q = 0; q < btm::kPhaseSlots; ++q) h.phase_ms[q] = 1e-6 * (double)tns[q];
+                const uint64_t t1 = tns[btm::kPhaseSlots], t2 = tns[btm::kPhaseSlots + 1];
+                h.solve_ms = t2 > t1 ? 1e-6 * (double)(t2 - t1) : 0.0;
+                h.finish_ms = (t0 && t2 > t0) ? 1e-6 * (double)(t2 - t0) : 0.0;
                 if (histDev[i]) {
                     int rows = std::min(h.residual_capacity, outv[4]);
                     ck(cudaMemcpy(h.residuals, histDev[i], sizeof(double) * 6 * rows, cudaMemcpyDeviceToHost), "hist");

@@ -25,6 +25,7 @@
 // A converged solve satisfies the FP64 discrete equations built from
 // FP32-rounded coefficients (relative perturbations of order 1e-7).
 #include "btm_common.h"
+#include <type_traits>
 #include "btm_team.cuh"
 #include "btm_bc.cuh"
 #include "btm_phases64.cuh"
@@ -1325,6 +1326,290 @@ constexpr int kBandRefresh = 4;
 constexpr double kDeliverFraction = 0.1;
 constexpr int kDeliverWindow = 2000;
 
+// ---------------------------------------------------------------------------
+// Anderson acceleration of the outer iteration.
+//
+// Within each stage the outer iteration is a fixed-point map G of the
+// interior state x = (U, p, k, omega) whose slowest modes (the bulk flow
+// rate against the wall shear, the near-wall k-omega balance) decay by less
+// than 1e-3 per outer iteration near convergence.  Anderson's method (type II, Walker & Ni, SIAM J.
+// Numer. Anal. 49 (2011) 1715) keeps the last m differences of the changes
+// f_i = W (G(x_i) - x_i) and of the results G(x_i), solves the small least
+// squares problem min |f_k - dF gamma| through its regularised normal
+// equations and continues from x_{k+1} = G(x_k) - dG gamma.  The fixed point
+// is that of the plain iteration; only the path to it changes.  The state
+// delivered at convergence is still G(x_k) of the iteration whose residuals
+// passed the test.  W weights each field by the inverse of its largest
+// magnitude (p by the inverse dynamic pressure), so no field dominates the
+// least squares problem by its units.
+//
+// Storage: the differences in FP32 (they only feed the least squares problem
+// and a correction of the size of one step), the iterate and the previous
+// result in FP64.  Each CTA's thread 0 keeps the Gram matrix of the stored
+// differences in shared memory and updates one row per iteration; in grid
+// mode every CTA holds an identical copy (the team reductions give every CTA
+// the same totals).
+constexpr double kAndersonReg = 1e-6;  // Tikhonov term relative to the mean Gram diagonal
+// The FP32-assembly stage starts its own Anderson history once the largest
+// scaled residual is below this value (with the turbulence model settled):
+// on the 4x128 Re_tau 550 channel the slowest parameter draws then reach the
+// stage switch in about 4-5k instead of 16-17k outer iterations; started
+// earlier (1e-2), during the start-up transient, it gains less on the slow
+// draws.  The history restarts at the stage switch (the map changes there).
+constexpr double kAndersonStart = 1e-3;
+// With a history running, the FP32-assembly stage counts as stalled after
+// this many iterations without a 10 % gain, anywhere below kAndersonStart:
+// where the FP32 coefficients' rounding noise stalls the accelerated
+// iteration, the FP64-assembly stage (whose map is smooth) takes over.
+constexpr int kStallWindowAnderson = 500;
+
+struct AndersonShared {
+    double G[kAndersonMax][kAndersonMax];
+    double gam[kAndersonMax];
+    double w[kAaFields];
+    int cnt;     // stored differences
+    int head;    // slot of the next difference
+    int have;    // a previous result exists
+};
+
+template <class T>
+__device__ __forceinline__ double *aa_field(DevInst &I, int v) {
+    switch (v) {
+        case 0: return I.ux;
+        case 1: return I.uy;
+        case 2: return I.uz;
+        case 3: return I.p;
+        case 4: return I.k;
+        default: return I.om;
+    }
+}
+
+// Start of a history (in the FP32-assembly stage once its residual is low,
+// again at the start of the FP64-assembly stage): weights from the current
+// state, the current state as the first iterate, no stored differences.
+template <class T>
+__device__ void aa_begin(T &tm, const DevMesh &M, DevInst &I, AndersonShared &sh) {
+    DevWork32 &F = I.f;
+    const int nC = M.nC;
+    float mx[3] = {0.0f, 0.0f, 0.0f};
+    for (int c = tm.rank(); c < nC; c += tm.size()) {
+        const double ux = LD(I.ux + c), uy = LD(I.uy + c), uz = I.solveZ ? LD(I.uz + c) : 0.0;
+        mx[0] = smaxf(mx[0], (float)sqrt(ux * ux + uy * uy + uz * uz));
+        mx[1] = smaxf(mx[1], (float)fabs(LD(I.k + c)));
+        mx[2] = smaxf(mx[2], (float)fabs(LD(I.om + c)));
+    }
+    tm.template maxf<3>(mx);
+    for (int v = 0; v < kAaFields; ++v) {
+        const double *phi = aa_field<T>(I, v);
+        if (v == 2 && !I.solveZ) continue;
+        for (int c = tm.rank(); c < nC; c += tm.size()) F.aaX[(size_t)v * nC + c] = LD(phi + c);
+    }
+    if (threadIdx.x == 0) {
+        const double um = mx[0] > 0.0f ? (double)mx[0] : 1.0;
+        sh.w[0] = sh.w[1] = sh.w[2] = 1.0 / um;
+        sh.w[3] = 2.0 / (um * um);
+        sh.w[4] = mx[1] > 0.0f ? 1.0 / (double)mx[1] : 1.0;
+        sh.w[5] = mx[2] > 0.0f ? 1.0 / (double)mx[2] : 1.0;
+        sh.cnt = 0;
+        sh.head = 0;
+        sh.have = 0;
+    }
+    tm.sync();
+}
+
+// Sixteen FP32 sums over the team (the grid team reduces four at a time).
+template <class T>
+__device__ __forceinline__ void aa_sum16(T &tm, float *v) {
+    if constexpr (std::is_same<T, GridTeam>::value) {
+        tm.template sumf<4>(v);
+        tm.template sumf<4>(v + 4);
+        tm.template sumf<4>(v + 8);
+        tm.template sumf<4>(v + 12);
+    } else {
+        tm.template sumf<8>(v);
+        tm.template sumf<8>(v + 8);
+    }
+}
+
+// Solve (G + reg I) gamma = b on the first n slots with warp 0 of the CTA:
+// lane i holds row i.  Cholesky by columns (one reciprocal square root per
+// pivot, the trailing update through shuffles; lane k keeps column k of the
+// factor as it is broadcast), then both triangular solves by columns.  Every
+// lane returns the same gamma and status.  (A serial factorisation on one
+// thread was 30 us per outer iteration at depth 8: dependent FP64 divisions
+// and square roots are slow on GB300.)
+__device__ __noinline__ bool aa_solve_warp(AndersonShared &sh, const float *bv, int n) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    double tr = 0.0;
+    for (int q = 0; q < n; ++q) tr += sh.G[q][q];
+    bool ok = tr > 0.0 && isfinite(tr);
+    const double reg = ok ? kAndersonReg * tr / n : 0.0;
+    double a[kAndersonMax], c[kAndersonMax], rinv[kAndersonMax];
+#pragma unroll
+    for (int q = 0; q < kAndersonMax; ++q) {
+        a[q] = (lane < n && q < n) ? sh.G[lane][q] : 0.0;
+        if (q == lane) a[q] += reg;
+        c[q] = 0.0;
+        rinv[q] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kAndersonMax; ++k) {
+        if (k < n) {
+            const double d = __shfl_sync(full, a[k], k);
+            if (!(d > 0.0) || !isfinite(d)) ok = false;
+            const double r = ok ? rsqrt(d) : 0.0;
+            rinv[k] = r;
+            const double lik = a[k] * r;   // L_ik in lane i >= k (L_kk in lane k)
+            a[k] = lik;
+#pragma unroll
+            for (int j = k + 1; j < kAndersonMax; ++j) {
+                if (j < n) {
+                    const double ljk = __shfl_sync(full, lik, j);
+                    a[j] = fma(-lik, ljk, a[j]);
+                    if (lane == k) c[j] = ljk;
+                }
+            }
+        }
+    }
+    // L y = b: lane i accumulates b_i - sum_{q<i} L_iq y_q and keeps y_i
+    double sacc = 0.0, t = 0.0;
+#pragma unroll
+    for (int q = 0; q < kAndersonMax; ++q)
+        if (q == lane) sacc = (double)bv[q];
+#pragma unroll
+    for (int k = 0; k < kAndersonMax; ++k) {
+        if (k < n) {
+            const double yk = __shfl_sync(full, sacc, k) * rinv[k];
+            if (lane == k) t = yk;
+            sacc = fma(-a[k], yk, sacc);
+        }
+    }
+    // L^T gamma = y: lane i accumulates y_i - sum_{q>i} L_qi gamma_q; lane 0
+    // writes gamma
+#pragma unroll
+    for (int k = kAndersonMax - 1; k >= 0; --k) {
+        if (k < n) {
+            const double gk = __shfl_sync(full, t, k) * rinv[k];
+            if (!isfinite(gk)) ok = false;
+            if (lane == 0) sh.gam[k] = gk;
+            t = fma(-c[k], gk, t);
+        }
+    }
+    return ok;
+}
+
+// One Anderson step after an outer iteration that did not end the solve: the state arrays hold G(x_k) on entry and x_{k+1}
+// (clamped like the iteration's own k and omega, boundary values re-applied)
+// on return.
+template <class T>
+__device__ void aa_step(T &tm, const DevMesh &M, DevInst &I, AndersonShared &sh, double beta1) {
+    DevWork32 &F = I.f;
+    const int nC = M.nC, depth = I.S.aaDepth;
+    const size_t len = (size_t)kAaFields * nC;
+    const bool have = sh.have != 0;
+    const int j = sh.head;
+    const int n = have ? min(sh.cnt + 1, depth) : 0;   // stored differences after this one
+    float acc[2 * kAndersonMax];
+#pragma unroll
+    for (int i = 0; i < 2 * kAndersonMax; ++i) acc[i] = 0.0f;
+    for (int v = 0; v < kAaFields; ++v) {
+        if (v == 2 && !I.solveZ) continue;
+        const double *phi = aa_field<T>(I, v);
+        const double w = sh.w[v];
+        for (int c = tm.rank(); c < nC; c += tm.size()) {
+            const size_t e = (size_t)v * nC + c;
+            const double g = LD(phi + c);
+            const float f = (float)(w * (g - F.aaX[e]));
+            if (have) {
+                const float df = f - F.aaFprev[e];
+                F.aaDF[j * len + e] = df;
+                F.aaDG[j * len + e] = (float)(g - F.aaGprev[e]);
+#pragma unroll
+                for (int i = 0; i < kAndersonMax; ++i) {
+                    if (i < n) {
+                        const float di = i == j ? df : F.aaDF[i * len + e];
+                        acc[i] = fmaf(di, df, acc[i]);
+                        acc[kAndersonMax + i] = fmaf(di, f, acc[kAndersonMax + i]);
+                    }
+                }
+            }
+            F.aaFprev[e] = f;
+            F.aaGprev[e] = g;
+        }
+    }
+    // (the reductions double as the barrier between every thread's reads of
+    // `sh` above and thread 0's updates below)
+    if (have) aa_sum16(tm, acc);
+    else __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        int use = 0;
+        if (have) {
+            // the new row and column of the Gram matrix
+            double gv = 0.0;
+#pragma unroll
+            for (int q = 0; q < kAndersonMax; ++q)
+                if (q == lane) gv = (double)acc[q];
+            if (lane < n) {
+                sh.G[j][lane] = gv;
+                sh.G[lane][j] = gv;
+            }
+            __syncwarp();
+            if (aa_solve_warp(sh, acc + kAndersonMax, n)) use = n;
+        }
+        if (lane == 0) {
+            if (use) {
+                sh.cnt = n;
+                sh.head = j + 1 == depth ? 0 : j + 1;
+            } else {
+                // no history yet, or a singular / non-finite system: restart it
+                sh.cnt = 0;
+                sh.head = 0;
+            }
+            for (int i = use; i < kAndersonMax; ++i) sh.gam[i] = 0.0;
+            sh.have = 1;
+        }
+    }
+    __syncthreads();
+    if (have && sh.cnt > 0) {
+        float gam[kAndersonMax];
+#pragma unroll
+        for (int i = 0; i < kAndersonMax; ++i) gam[i] = (float)sh.gam[i];
+        const double kLo = I.S.kMin, kHi = I.S.kMax, wLo = I.S.omegaMin;
+        for (int v = 0; v < kAaFields; ++v) {
+            if (v == 2 && !I.solveZ) continue;
+            double *phi = aa_field<T>(I, v);
+            for (int c = tm.rank(); c < nC; c += tm.size()) {
+                const size_t e = (size_t)v * nC + c;
+                float corr = 0.0f;
+#pragma unroll
+                for (int i = 0; i < kAndersonMax; ++i)
+                    if (i < n) corr = fmaf(gam[i], F.aaDG[i * len + e], corr);
+                double x = F.aaGprev[e] - (double)corr;
+                if (v == 4) x = smax(kLo, smin(kHi, x));
+                else if (v == 5) x = smax(wLo, smin(1e15, x));
+                phi[c] = x;
+                F.aaX[e] = x;
+            }
+        }
+        tm.sync();
+        phase_bc_u(tm, M, I);
+        phase_bc_p(tm, M, I);
+        phase_bc_k(tm, M, I, true);
+        phase_bc_w(tm, M, I, beta1, true);
+        tm.sync();
+    } else {
+        for (int v = 0; v < kAaFields; ++v) {
+            if (v == 2 && !I.solveZ) continue;
+            for (int c = tm.rank(); c < nC; c += tm.size()) {
+                const size_t e = (size_t)v * nC + c;
+                F.aaX[e] = F.aaGprev[e];
+            }
+        }
+    }
+}
+
 template <class T>
 __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     const DevSettings &S = I.S;
@@ -1355,6 +1640,9 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
     PhaseClock clk;
     clk.start(tm.leader());
     const uint64_t tStart = tm.leader() ? globaltimer_ns() : 0;
+    __shared__ AndersonShared aa;
+    const bool aaOn = S.aaDepth > 0;
+    bool aaRun = false;        // an Anderson history of the current stage exists
 
     for (int iter = 0; iter < S.maxIter; ++iter) {
         if (!tm.ok()) break;
@@ -1630,11 +1918,12 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         if (!polish) {
             winBest = smin(winBest, maxRes);
             bool stalled = false;
-            if (iter + 1 - winStart >= kStallWindow) {
+            if (iter + 1 - winStart >= (aaRun ? kStallWindowAnderson : kStallWindow)) {
                 // a warm start normalised by its own (small) first defects can
                 // sit on the FP32 floor at any scaled residual
                 const bool ownScale = I.initMode != 0 && !I.normFixed;
-                stalled = settled && !(winBest < kStallGain * bestRes) && (ownScale || winBest < kStallCeiling);
+                const double ceiling = aaRun ? kAndersonStart : kStallCeiling;
+                stalled = settled && !(winBest < kStallGain * bestRes) && (ownScale || winBest < ceiling);
                 bestRes = smin(bestRes, winBest);
                 winBest = INFINITY;
                 winStart = iter + 1;
@@ -1649,7 +1938,24 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
                 tm.sync();
                 polish = true;
                 polishStart = iter + 1;
+                if (aaOn) {
+                    aa_begin(tm, M, I, aa);
+                    aaRun = true;
+                }
+            } else if (aaOn && !aaRun && settled && maxRes < kAndersonStart) {
+                aa_begin(tm, M, I, aa);
+                aaRun = true;
+            } else if (aaRun && iter + 1 < S.maxIter) {
+                clk.lap(9);
+                aa_step(tm, M, I, aa, b1);
+                clk.lap(8);
             }
+        } else if (aaRun && iter + 1 < S.maxIter) {
+            // (not after the last iteration: a solve that ends at the cap
+            // delivers G(x_k) like one that converges)
+            clk.lap(9);
+            aa_step(tm, M, I, aa, b1);
+            clk.lap(8);
         }
     }
     if (!converged && !diverged && passedNow) {
@@ -1685,9 +1991,9 @@ __device__ void mixed_solve(T &tm, const DevMesh &M, DevInst &I) {
         I.outLast[6] = normUx0;
         I.outLast[7] = normUy0;
         I.outLast[8] = normP0;
-        for (int q = 0; q < 8; ++q) I.outTime[q] = clk.acc[q];
-        I.outTime[8] = tStart;
-        I.outTime[9] = globaltimer_ns();
+        for (int q = 0; q < kPhaseSlots; ++q) I.outTime[q] = clk.acc[q];
+        I.outTime[kPhaseSlots] = tStart;
+        I.outTime[kPhaseSlots + 1] = globaltimer_ns();
         if (I.obsOut) observe_leader<T>(M, I);
         if (I.doneFlag) {
             __threadfence_system();

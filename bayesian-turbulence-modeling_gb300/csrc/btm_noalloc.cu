@@ -241,7 +241,7 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
     int64_t innerv[5] = {0, 0, 0, 0, 0};
     int32_t errv = 0;
     double lastv[6] = {0};
-    uint64_t tns[10] = {0};
+    uint64_t tns[btm::kPhaseSlots + 2] = {0};
     bool ok = ck(cudaMemcpyAsync(outv, I.out, sizeof outv, cudaMemcpyDeviceToHost, st), "status") &&
               ck(cudaMemcpyAsync(innerv, I.outInner, sizeof innerv, cudaMemcpyDeviceToHost, st), "status") &&
               ck(cudaMemcpyAsync(lastv, I.outLast, sizeof lastv, cudaMemcpyDeviceToHost, st), "status") &&
@@ -296,8 +296,9 @@ extern "C" int btm_solve_noalloc(btm_case *C, const double *coeffs, int32_t vari
         for (int q = 0; q < 4; ++q) hist->inner_split[q] = innerv[q + 1];
         hist->polish_start = outv[7];
         for (int q = 0; q < 6; ++q) hist->last_residual[q] = lastv[q];
-        for (int q = 0; q < 8; ++q) hist->phase_ms[q] = 1e-6 * (double)tns[q];
-        hist->solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
+        for (int q = 0; q < btm::kPhaseSlots; ++q) hist->phase_ms[q] = 1e-6 * (double)tns[q];
+        hist->solve_ms = tns[btm::kPhaseSlots + 1] > tns[btm::kPhaseSlots]
+                           ? 1e-6 * (double)(tns[btm::kPhaseSlots + 1] - tns[btm::kPhaseSlots]) : 0.0;
         hist->finish_ms = hist->solve_ms;
         if (nObs > 0) {
             for (int q = 0; q < nObs; ++q) hist->predictions[q] = obsv[q];

@@ -172,7 +172,7 @@ void complete(btm_server *S, Slot &s) {
     int32_t outv[8];
     int64_t innerv[5];
     double lastv[9];
-    uint64_t tns[10];
+    uint64_t tns[btm::kPhaseSlots + 2];
     int32_t errv = 0;
     cudaStream_t st = S->copyStream;
     sck(cudaMemcpyAsync(outv, I.out, sizeof outv, cudaMemcpyDeviceToHost, st), "status");
@@ -191,8 +191,9 @@ void complete(btm_server *S, Slot &s) {
         for (int q = 0; q < 4; ++q) h->inner_split[q] = innerv[q + 1];
         h->polish_start = outv[7];
         for (int q = 0; q < 6; ++q) h->last_residual[q] = lastv[q];
-        for (int q = 0; q < 8; ++q) h->phase_ms[q] = 1e-6 * (double)tns[q];
-        h->solve_ms = tns[9] > tns[8] ? 1e-6 * (double)(tns[9] - tns[8]) : 0.0;
+        for (int q = 0; q < btm::kPhaseSlots; ++q) h->phase_ms[q] = 1e-6 * (double)tns[q];
+        h->solve_ms = tns[btm::kPhaseSlots + 1] > tns[btm::kPhaseSlots]
+                           ? 1e-6 * (double)(tns[btm::kPhaseSlots + 1] - tns[btm::kPhaseSlots]) : 0.0;
         h->finish_ms = h->solve_ms;
         btm_host::download_obs(s.C, I, h, st);
     }

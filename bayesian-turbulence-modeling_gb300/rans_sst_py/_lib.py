@@ -47,7 +47,7 @@ class BtmSettings(C.Structure):
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
                 ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double),
-                ("amg_order", C.c_int32)]
+                ("amg_order", C.c_int32), ("anderson_depth", C.c_int32)]
 
 
 class BtmState(C.Structure):
@@ -64,7 +64,7 @@ class BtmHistory(C.Structure):
     _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
                 ("final_iter", C.c_int32), ("iterations_run", C.c_int32),
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
-                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8),
+                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 10),
                 ("solve_ms", C.c_double), ("finish_ms", C.c_double), ("inner_split", C.c_int64 * 4),
                 ("polish_start", C.c_int32), ("predictions", _dp), ("log_lik", C.c_double)]
 
@@ -79,6 +79,7 @@ class BtmObservable(C.Structure):
 SOLVER_CODES = {"PCG": 0, "BiCGSTAB": 1, "GaussSeidel": 2, "AMG": 3}
 PRECISION_CODES = {"fp64": 0, "mixed": 1}
 AMG_ORDER_CODES = {"auto": 0, "reference": 1, "multicolour": 2}
+ANDERSON_DEPTH_DEFAULT = 8   # SolverSettings.anderson_depth
 PHASES = {"grad": 1, "sst": 2, "momentum": 3, "pressure": 4, "k": 5, "omega": 6, "spmv": 7,
           "bicgstab": 8, "amgpcg": 9, "pcg": 11, "amg_levels": 12, "gs": 13}
 
@@ -228,6 +229,7 @@ def settings_struct(s) -> BtmSettings:
     if order not in AMG_ORDER_CODES:
         raise ValueError(f"amg_order must be one of {sorted(AMG_ORDER_CODES)}, not {order!r}")
     st.amg_order = AMG_ORDER_CODES[order]
+    st.anderson_depth = int(getattr(s, "anderson_depth", ANDERSON_DEPTH_DEFAULT))
     return st
 
 

@@ -186,7 +186,10 @@ class SolverSettings:
     `precision` ("fp64", the reference's arithmetic, or "mixed": FP32 bulk
     with FP64 state, defects and refinement) selects the device engine, and
     `amg_order` ("auto", "reference" or "multicolour") the form of the FP64
-    engine's AMG-preconditioned CG (BTM_AMG_* in the C header)."""
+    engine's AMG-preconditioned CG (BTM_AMG_* in the C header), and
+    `anderson_depth` (0 .. 8) the depth of the Anderson acceleration of the
+    mixed engine's outer iteration (0: plain SIMPLE iterations; the FP64
+    engine, the reference's drop-in, ignores it)."""
 
     def __init__(self):
         self.max_iterations = 500
@@ -219,6 +222,7 @@ class SolverSettings:
         self.sst_variant = 0
         self.precision = "fp64"
         self.amg_order = "auto"
+        self.anderson_depth = 8
 
     def copy(self) -> "SolverSettings":
         s = SolverSettings()

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define BTM_ABI_VERSION 5
+#define BTM_ABI_VERSION 6
 
 /* ---- status codes -------------------------------------------------------- */
 #define BTM_OK              0
@@ -178,7 +178,14 @@ typedef struct btm_settings {
     double  alpha_injection;       /* blend factor of the Reynolds-stress
                                       injection source (alphaInjection) */
     int32_t amg_order;             /* BTM_AMG_*; not a reference field */
+    int32_t anderson_depth;        /* mixed engine: depth of the Anderson
+                                      acceleration of its outer iteration
+                                      (from a scaled residual of 1e-3 on, and
+                                      afresh in the FP64-assembly stage),
+                                      0 (off) .. BTM_ANDERSON_MAX; ignored by
+                                      the FP64 engine; not a reference field */
 } btm_settings;
+#define BTM_ANDERSON_MAX 8
 
 /* Initial state.  mode 0 = cold uniform start exactly as
  * SIMPLESolver::initUniform (SIMPLESolver.cpp:23-51); mode 1 = warm start from
@@ -223,9 +230,12 @@ typedef struct btm_history {
     double *residuals;             /* [residual_capacity*6] or NULL            */
     /* device time per phase in ms, the reference's per-solve phase timers
      * (SIMPLESolver.hpp:123-136): [0] SST closure, [1] momentum assembly,
-     * [2] momentum solves, [3] p' assembly, [4] AMG numeric setup,
-     * [5] p' solve, [6] corrections + BCs, [7] k/omega assembly+solves */
-    double  phase_ms[8];
+     * [2] momentum solves, [3] p' assembly, [4] p' solver setup (AMG
+     * numeric setup, band factorisation), [5] p' solve, [6] corrections +
+     * BCs, [7] k/omega assembly+solves, [8] the mixed engine's Anderson
+     * update, [9] residual bookkeeping and convergence tests of the mixed
+     * engine's FP64-assembly stage */
+    double  phase_ms[10];
     /* device time of this instance from the start of its solve to its end,
      * and its end relative to the earliest instance start of the same
      * launch (the latency of a request submitted with the batch) */

@@ -42,7 +42,7 @@ class Settings(C.Structure):
                 ("von_karman", C.c_double), ("wall_fn_E", C.c_double),
                 ("pressure_solver", C.c_int32), ("momentum_solver", C.c_int32),
                 ("turbulence_solver", C.c_int32), ("precision", C.c_int32), ("alpha_injection", C.c_double),
-                ("amg_order", C.c_int32)]
+                ("amg_order", C.c_int32), ("anderson_depth", C.c_int32)]
 
 
 class State(C.Structure):
@@ -59,7 +59,7 @@ class History(C.Structure):
     _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
                 ("final_iter", C.c_int32), ("iterations_run", C.c_int32),
                 ("inner_iterations", C.c_int64), ("last_residual", C.c_double * 6),
-                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 8),
+                ("residual_capacity", C.c_int32), ("residuals", _dp), ("phase_ms", C.c_double * 10),
                 ("solve_ms", C.c_double), ("finish_ms", C.c_double), ("inner_split", C.c_int64 * 4),
                 ("polish_start", C.c_int32), ("predictions", C.POINTER(C.c_double)), ("log_lik", C.c_double)]
 

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     missing = [s for s in declared_symbols() if not hasattr(lib, s)]
     assert not missing, f"not exported: {missing}"
     lib.btm_abi_version.restype = ctypes.c_int
-    assert lib.btm_abi_version() == 5
+    assert lib.btm_abi_version() == 6
 
 
 def test_build_targets_sm103a_only():
