@@ -2172,14 +2172,21 @@ size_t mixed_smem_bytes(int nC, int nIF, int64_t vecTotal, int64_t valTotal, int
 // leaves the CTAs-per-SM of the launch bounds resident.
 int mixed_launch_block(DevInst *dInsts, int n, int threads, size_t smemBytes, void *stream) {
     if (n <= 0) return 0;
-    int dev = 0, perSm = 0;
+    int dev = 0, perSm = 0, perBlock = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&perBlock, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&fa, threads == 256 ? (const void *)k_mixed_block<256> : (const void *)k_mixed_block<512>);
     if (e != cudaSuccess) return (int)e;
     const int ctas = 512 / threads;
-    // static shared memory of the kernel plus the per-CTA reservation
-    const size_t reserve = 8 * 1024;
-    size_t cap = (size_t)perSm / ctas > reserve ? (size_t)perSm / ctas - reserve : 0;
+    // per CTA: at most the opt-in block limit and its share of the SM (less
+    // the runtime's 1 KB reservation per CTA), static shared memory included
+    const size_t kCtaReserve = 1024;
+    size_t total = (size_t)perSm / ctas > kCtaReserve ? (size_t)perSm / ctas - kCtaReserve : 0;
+    if (total > (size_t)perBlock) total = (size_t)perBlock;
+    const size_t cap = total > fa.sharedSizeBytes ? total - fa.sharedSizeBytes : 0;
     if (smemBytes > cap) smemBytes = cap;
     smemBytes &= ~size_t(kSmemAlign - 1);
     if (threads == 256) {
