@@ -52,6 +52,10 @@ def _rel(a, b):
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 1e-5)])
 def test_injection_short_vs_oracle(golden, oracle, precision, tol):
     m, bcs, nu, s, init, c = _case(golden, precision, 60, 0.0, inner_tol=1e-12)
+    # the plain mixed iteration: Anderson acceleration changes the path (not
+    # the fixed point), so a trajectory comparison runs without it
+    s.anderson_depth = 0
+    c.set_settings(s)
     out = solve(c, cases.COEFF_DEFAULTS, 0, init)
     ref, _ = oracle.solve(m, bcs, nu, s, cases.COEFF_DEFAULTS, 0, **init, b_target=golden["b_target"])
     for f in ("U", "k", "omega", "nuT"):

@@ -230,6 +230,9 @@ def _bfs_warm_from_reference(precision, iters):
     m = mesh_from(g)
     s = settings_from(g)
     s.max_iterations, s.convergence_tol, s.precision = iters, 0.0, precision
+    # a continuation compared with the reference's own: the plain mixed
+    # iteration (Anderson acceleration changes the path, not the fixed point)
+    s.anderson_depth = 0
     ini = init_from(g)
     case = Case(m, FlowBoundaryConditions.bfs_defaults(m, 1.0, ini["k"], ini["omega"]), float(g["nu"]), s)
     warm = {f: np.array(g[f"conv_{f}"]) for f in ("U", "p", "k", "omega", "nuT", "F1", "F2", "Pk", "CDkw",
