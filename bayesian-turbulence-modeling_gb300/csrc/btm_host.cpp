@@ -1475,6 +1475,7 @@ int btm_case_set_observations(btm_case *C, const btm_mesh *m, int32_t n, const b
 struct CallResources {
     std::vector<void *> dev;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> joins;   // fork / join events of concurrent group launches
     CallResources() = default;
     CallResources(const CallResources &) = delete;
     CallResources &operator=(const CallResources &) = delete;
@@ -1483,8 +1484,28 @@ struct CallResources {
             if (p) cudaFree(p);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : joins)
+            if (e) cudaEventDestroy(e);
     }
 };
+
+// Streams on which the launch groups of one batch (instances of different
+// engines or CTA sizes) run side by side: a few per device, created on first
+// use and kept for the life of the process.  Calls from several host threads
+// may share them; their work then queues behind each other, which changes
+// timing only.
+constexpr int kGroupStreams = 4;
+cudaStream_t group_stream(int k) {
+    static std::mutex mtx;
+    static std::vector<std::array<cudaStream_t, kGroupStreams>> pool;
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mtx);
+    if ((int)pool.size() <= dev) pool.resize(dev + 1, std::array<cudaStream_t, kGroupStreams>{});
+    cudaStream_t &s = pool[dev][k % kGroupStreams];
+    if (!s) ck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate(group)");
+    return s;
+}
 
 int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, const int32_t *variants,
                     const btm_init *inits, btm_state *outs, btm_history *hists) {
@@ -1594,8 +1615,18 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
             res.dev.push_back(dInsts);
             ck(cudaMemcpyAsync(dInsts, arr.data(), sizeof(btm::DevInst) * arr.size(), cudaMemcpyHostToDevice, st), "insts");
             ck(cudaEventRecord(ev0, st), "event");
+            // more than one group: each on its own stream, forked from and
+            // joined back into the call's stream, so the groups run at the
+            // same time instead of one after the other
+            const bool fork = groups.size() > 1;
             size_t at = 0;
-            for (const Group &g : groups) {
+            for (size_t gi = 0; gi < groups.size(); ++gi) {
+                const Group &g = groups[gi];
+                cudaStream_t gs = st;
+                if (fork) {
+                    gs = group_stream((int)gi);
+                    ck(cudaStreamWaitEvent(gs, ev0, 0), "fork");
+                }
                 int maxCells = 0;
                 bool refAmg = false;
                 size_t smem = 0;
@@ -1609,9 +1640,16 @@ int btm_solve_batch(int32_t n, btm_case *const *cases, const double *coeffs, con
                                                                     Cm->dmesh.band));
                 }
                 const int e = g.engine == 0
-                                  ? btm::engine_launch_block(dInsts + at, (int)g.idx.size(), g.threads, st, refAmg, maxCells)
-                                  : btm::mixed_launch_block(dInsts + at, (int)g.idx.size(), g.threads, smem, st);
+                                  ? btm::engine_launch_block(dInsts + at, (int)g.idx.size(), g.threads, gs, refAmg, maxCells)
+                                  : btm::mixed_launch_block(dInsts + at, (int)g.idx.size(), g.threads, smem, gs);
                 if (e) throw BtmError(BTM_ERR_CUDA, std::string("block launch: ") + cudaGetErrorString((cudaError_t)e));
+                if (fork) {
+                    cudaEvent_t j = nullptr;
+                    ck(cudaEventCreateWithFlags(&j, cudaEventDisableTiming), "event");
+                    res.joins.push_back(j);
+                    ck(cudaEventRecord(j, gs), "join");
+                    ck(cudaStreamWaitEvent(st, j, 0), "join");
+                }
                 at += g.idx.size();
             }
         } else {

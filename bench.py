@@ -722,6 +722,97 @@ def run_large(args):
     print(json.dumps(line), flush=True)
 
 
+# The batched mixed-precision mesh mix: streamwise-periodic 4 x ny channels,
+# first cell at y+ 0.4 except the 4x128 Re_tau 550 channel of the headline
+# (ratio 1.08): (wall-normal cells, Re_tau, ratio).
+C3_MESHES = [(64, 180.0, None), (128, 550.0, 1.08), (256, 1000.0, None), (512, 2000.0, None)]
+C3_MAX_ITER = 200000
+C3_FP64_CHECK = 2            # instances per mesh checked against the FP64 engine
+C3_FP64_ITERS = 40000        # FP64 outer iterations continued from each checked mixed result
+
+
+def run_c3(args):
+    """The 256-theta draw spread over four channel meshes (theta i on mesh
+    i mod 4; out-of-bounds draws are InvalidParameters and not solved), all
+    valid instances in one call: cold starts to the 1e-8 scaled residual in
+    the mixed engine.  Instances of different CTA sizes run as concurrent
+    launches.  After the timed steps the first C3_FP64_CHECK instances of
+    every mesh are continued by the FP64 engine for C3_FP64_ITERS iterations
+    (convergence test off): the distance the FP64 iteration moves them is
+    their distance to its fixed point where that iteration converges within
+    the count (meshes up to Re_tau 1000 here; the reference algorithm does not
+    converge on the Re_tau 2000 mesh from the cold start within 200k
+    iterations)."""
+    import rans_sst_py as rs
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases as tc
+    _, coeffs, valid = theta_set()
+    mesh_cases, by_mesh = [], []
+    for ny, re, ratio in C3_MESHES:
+        m, bcs, nu, init = tc.periodic_channel(ny, re, ratio=ratio)
+        s = tc.channel_settings(C3_MAX_ITER, TOL)
+        s.precision = "mixed"
+        mesh_cases.append((m, bcs, nu, init, rs.Case(m, bcs, nu, s)))
+    ids = [i for i in range(N_THETA) if valid[i]]
+    tags = [i % len(C3_MESHES) for i in ids]
+    batch = [mesh_cases[t][4] for t in tags]
+    inits = [mesh_cases[t][3] for t in tags]
+    cf = coeffs[ids]
+
+    def step():
+        t0 = time.perf_counter()
+        outs = rs.solve_batch(batch, cf, None, inits, want_state=True)
+        return outs, lib_launch_ms(), time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    dev_ms, wall_s = [], []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            outs, ms, wall = step()
+            dev_ms.append(ms)
+            wall_s.append(wall)
+    conv = sum(o.converged for o in outs)
+    per_mesh = []
+    for t, (ny, re, _) in enumerate(C3_MESHES):
+        mo = [o for o, tg in zip(outs, tags) if tg == t]
+        it = np.array([o.iterations_run for o in mo])
+        fin = np.array([o.finish_ms for o in mo])
+        per_mesh.append({"mesh": f"4x{ny}", "re_tau": re, "cells": mesh_cases[t][0].n_cells(), "instances": len(mo),
+                         "converged": int(sum(o.converged for o in mo)), "iters_mean": float(it.mean()),
+                         "iters_max": int(it.max()), "finish_ms_p50": float(np.percentile(fin, 50)),
+                         "finish_ms_max": float(fin.max())})
+    # FP64 continuation of the first instances of every mesh, one batch
+    chk, chk_cases, chk_cf, chk_warm = [], [], [], []
+    for t in range(len(C3_MESHES)):
+        m, bcs, nu, _, _ = mesh_cases[t]
+        s = tc.channel_settings(C3_FP64_ITERS, 0.0)
+        c = rs.Case(m, bcs, nu, s)
+        for j in [j for j, tg in enumerate(tags) if tg == t][:C3_FP64_CHECK]:
+            chk.append((t, j))
+            chk_cases.append(c)
+            chk_cf.append(cf[j])
+            chk_warm.append(outs[j].state)
+    fps = rs.solve_batch(chk_cases, np.array(chk_cf), None, chk_warm, want_state=True)
+    for (t, j), f in zip(chk, fps):
+        d = {k: float(np.linalg.norm(outs[j].state[k] - f.state[k]) / np.linalg.norm(f.state[k]))
+             for k in ("U", "k", "omega", "nuT")}
+        per_mesh[t].setdefault("distance_to_fp64_continuation", []).append(d)
+    step_ms = statistics.mean(dev_ms)
+    line = {"metric": "converged RANS solves/sec", "value": conv / (step_ms * 1e-3), "unit": "solves/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic", "impl": "gb300",
+            "config": {"workload": "c3_theta256_channels_4x64_128_256_512_re180_550_1000_2000", "precision": "mixed",
+                       "n_theta": N_THETA, "n_valid": len(ids), "tol": TOL, "max_iterations": C3_MAX_ITER},
+            "converged_per_step": int(conv),
+            "e2e": {"value": conv / statistics.mean(wall_s), "unit": "solves/s"},
+            "per_mesh": per_mesh, "clocks": clocks.summary(),
+            "fp64_check": {"instances_per_mesh": C3_FP64_CHECK, "fp64_iterations": C3_FP64_ITERS,
+                           "note": "relative L2 between each mixed result and the FP64 engine continued from it"}}
+    print(json.dumps(line), flush=True)
+
+
 def lib_launch_ms():
     from rans_sst_py._lib import lib
     return float(lib().btm_last_launch_ms())
@@ -749,12 +840,19 @@ def main():
     ap.add_argument("--large-iters", type=int, default=20, help="--large: outer iterations from the cold start")
     ap.add_argument("--large-precision", choices=["fp64", "mixed"], default=None,
                     help="--large: engine (default fp64 for bfs120k, mixed for duct2m)")
+    ap.add_argument("--c3", action="store_true",
+                    help="the 256-theta mesh mix over the 4x64/128/256/512 channels instead of the batch "
+                         "(give --warmup 1: one step takes about a minute)")
     args = ap.parse_args()
     global PRECISION
     PRECISION = args.precision
     world, rank, local = dist_setup()
     if args.profile_case:
         run_profile_case()
+        return
+    if args.c3:
+        if rank == 0:
+            run_c3(args)
         return
     if args.served:
         if rank == 0:
