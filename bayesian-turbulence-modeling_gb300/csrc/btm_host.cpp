@@ -1068,6 +1068,7 @@ int block_threads_for(int maxCells) {
 // in any batch.  BTM_BLOCK_THREADS=256|512 forces a shape, BTM_AUTOTUNE=0
 // keeps the size rule (256 threads up to BTM_SMALL_CELLS cells).
 constexpr int kTuneIters = 40;
+constexpr int kTuneRepeats = 2;                     // timed launches per shape
 constexpr size_t kTuneBytes = size_t(512) << 20;   // device memory the probe slabs may take
 
 int case_threads(const btm_case *C, int engine) {
@@ -1122,16 +1123,27 @@ void autotune_case(btm_case *C, const double *coeffs, int variant) {
         const size_t smem = engine == 1 ? btm::mixed_smem_bytes(C->nC, C->nIF, C->amgVecTotal, C->amgValTotal,
                                                                 C->dmesh.coarseDirect ? C->amgCoarseN : 1, C->dmesh.band)
                                         : 0;
-        float ms[2] = {0.0f, 0.0f};
         const int shapes[2] = {256, 512};
-        for (int k = 0; k < 2; ++k) {
-            ck(cudaEventRecord(ev[0], st), "event");
-            const int e = engine == 0 ? btm::engine_launch_block(d, nProbe, shapes[k], st, refAmg, C->nC)
-                                      : btm::mixed_launch_block(d, nProbe, shapes[k], smem, st);
+        auto launch = [&](int k, int n) {
+            const int e = engine == 0 ? btm::engine_launch_block(d, n, shapes[k], st, refAmg, C->nC)
+                                      : btm::mixed_launch_block(d, n, shapes[k], smem, st);
             if (e) throw BtmError(BTM_ERR_CUDA, std::string("tune launch: ") + cudaGetErrorString((cudaError_t)e));
+        };
+        // one untimed single-instance launch per shape first (module load,
+        // shared-memory attributes), then each shape timed twice in
+        // alternating order; the faster time of each counts
+        for (int k = 0; k < 2; ++k) launch(k, 1);
+        ck(cudaStreamSynchronize(st), "tune");
+        float ms[2] = {0.0f, 0.0f};
+        for (int rep = 0; rep < 2 * kTuneRepeats; ++rep) {
+            const int k = (rep & 1) ^ ((rep >> 1) & 1);   // 256, 512, 512, 256, ...
+            ck(cudaEventRecord(ev[0], st), "event");
+            launch(k, nProbe);
             ck(cudaEventRecord(ev[1], st), "event");
             ck(cudaStreamSynchronize(st), "tune");
-            ck(cudaEventElapsedTime(&ms[k], ev[0], ev[1]), "event time");
+            float t = 0.0f;
+            ck(cudaEventElapsedTime(&t, ev[0], ev[1]), "event time");
+            if (ms[k] == 0.0f || t < ms[k]) ms[k] = t;
         }
         C->tuneMs[engine][0] = ms[0];
         C->tuneMs[engine][1] = ms[1];
