@@ -35,6 +35,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import multiprocessing as mp
 import os
 import statistics
@@ -479,16 +480,6 @@ def run_gpu(args, world, rank, local):
                               "latency_ms": {"p50": float(np.percentile(fin64, 50)),
                                              "p99": float(np.percentile(fin64, 99))},
                               "speedup_of_mixed": value / (conv64 / (ms64 / 1e3))}
-        # the FP64 drop-in at a tenth of the tolerance: the same accuracy
-        # against the fixed point as the mixed engine's delivery rule
-        s64t = s64.copy()
-        s64t.convergence_tol = 0.1 * s64.convergence_tol
-        outs64t, ms64t, _ = step(rs.Case(m, bcs, nu, s64t))
-        conv64t, _ = _batch_stats(outs64t)
-        line["fp64_plain_equal_accuracy"] = {
-            "value": conv64t / (ms64t / 1e3), "unit": "solves/s", "ms": ms64t, "converged": conv64t, "tol": s64t.convergence_tol,
-            "iters_per_converged_solve": sum(o.iterations_run for o in outs64t) / n,
-            "speedup_of_mixed": value / (conv64t / (ms64t / 1e3))}
         # the FP64 fixed point of every instance (the FP64 engine, pinned to
         # the reference at stagnation, run well past convergence with the
         # test off): the error of what each engine delivers against it, per
@@ -505,9 +496,27 @@ def run_gpu(args, world, rank, local):
         e64.update(_output_errors(m, nu, outs64, outs_fp))
         e64["note"] = "the FP64 drop-in stopped by the reference's 1e-8 test, against the same fixed point"
         line["fp64_plain"]["error_vs_fp64_fixed_point"] = e64
+        # the FP64 drop-in at the tolerance that gives it the accuracy the
+        # mixed solves are delivered with: the distance to the fixed point is
+        # proportional to the tolerance, so the tolerance is scaled by the
+        # ratio of the two errors (largest over U, k, nu_t) and rounded down
+        # to a power of ten
+        worst = lambda e: max(e[f]["max"] for f in ("U", "k", "nuT"))  # noqa: E731
+        ratio = worst(e64) / max(worst(ev), 1e-300)
+        tol_eq = 10.0 ** math.floor(math.log10(s64.convergence_tol / max(ratio, 1.0)))
+        s64t = s64.copy()
+        s64t.convergence_tol = tol_eq
+        outs64t, ms64t, _ = step(rs.Case(m, bcs, nu, s64t))
+        conv64t, _ = _batch_stats(outs64t)
         e64t = _field_errors(outs64t, outs_fp)
         e64t.update(_output_errors(m, nu, outs64t, outs_fp))
-        line["fp64_plain_equal_accuracy"]["error_vs_fp64_fixed_point"] = e64t
+        line["fp64_plain_equal_accuracy"] = {
+            "value": conv64t / (ms64t / 1e3), "unit": "solves/s", "ms": ms64t, "converged": conv64t,
+            "tol": tol_eq, "iters_per_converged_solve": sum(o.iterations_run for o in outs64t) / n,
+            "speedup_of_mixed": value / max(conv64t / (ms64t / 1e3), 1e-300),
+            "error_vs_fp64_fixed_point": e64t,
+            "note": "the FP64 drop-in at the power-of-ten tolerance below 1e-8 / (its error at 1e-8 over the "
+                    "mixed solves' error): at least the accuracy the mixed solves are delivered with"}
         # precision error proper: a subset run to stagnation (convergence test
         # off, well past the converged iteration count) in both engines
         sub = list(range(0, n, max(1, n // FIXED_POINT_SUBSET)))[:FIXED_POINT_SUBSET]
