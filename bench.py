@@ -159,6 +159,7 @@ TRAFFIC_PER_CELL_ITER = {"fp64": 460.0, "mixed": 49.4}
 FIXED_POINT_SUBSET = 8
 FIXED_POINT_ITERS = 40000
 FIXED_POINT_STAG_ITERS = 60000
+FP64_RESIDUAL_FLOOR = 1e-10   # lowest tolerance the FP64 drop-in reaches on the 4x128 channel
 
 
 def algorithmic_bytes(n_cells, outer, inner, mixed=False):
@@ -500,11 +501,14 @@ def run_gpu(args, world, rank, local):
         # mixed solves are delivered with: the distance to the fixed point is
         # proportional to the tolerance, so the tolerance is scaled by the
         # ratio of the two errors (largest over U, k, nu_t) and rounded to the
-        # nearest power of ten (not below 1e-11, above the FP64 iteration's
-        # own residual floor on this mesh)
+        # nearest power of ten, but not below FP64_RESIDUAL_FLOOR: the
+        # reference iteration's scaled continuity residual settles at 3-7e-11
+        # on this mesh (it reaches 1e-10 after 20-37k outer iterations and
+        # 1e-11 never), so below that the leg is a lower bound of the speed-up
+        # at equal accuracy and its own error is reported beside it
         worst = lambda e: max(e[f]["max"] for f in ("U", "k", "nuT"))  # noqa: E731
         ratio = worst(e64) / max(worst(ev), 1e-300)
-        tol_eq = max(10.0 ** round(math.log10(s64.convergence_tol / max(ratio, 1.0))), 1e-11)
+        tol_eq = max(10.0 ** round(math.log10(s64.convergence_tol / max(ratio, 1.0))), FP64_RESIDUAL_FLOOR)
         s64t = s64.copy()
         s64t.convergence_tol = tol_eq
         s64t.max_iterations = 2 * MAX_ITER
@@ -519,7 +523,8 @@ def run_gpu(args, world, rank, local):
             "speedup_of_mixed": value / v64t if conv64t else None,
             "error_vs_fp64_fixed_point": e64t,
             "note": "the FP64 drop-in at the power of ten nearest to 1e-8 / (its error at 1e-8 over the mixed "
-                    "solves' error): about the accuracy the mixed solves are delivered with"}
+                    "solves' error), not below its residual floor (1e-10): at most the accuracy the mixed solves "
+                    "are delivered with, so the speed-up is a lower bound at equal accuracy"}
         # precision error proper: a subset run to stagnation (convergence test
         # off, well past the converged iteration count) in both engines
         sub = list(range(0, n, max(1, n // FIXED_POINT_SUBSET)))[:FIXED_POINT_SUBSET]
