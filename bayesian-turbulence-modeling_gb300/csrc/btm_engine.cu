@@ -17,6 +17,7 @@
 // (parallel trees) and transcendental library calls differ in the last bits.
 // There are no floating-point atomics anywhere.
 #include "btm_common.h"
+#include <type_traits>
 #include "btm_team.cuh"
 #include "btm_bc.cuh"
 #include "btm_phases64.cuh"
@@ -407,6 +408,14 @@ __device__ __noinline__ SolveResult team_amg_pcg(T &tm, const DevMesh &M, DevIns
     const double r0 = sqrt(a0[0]);
     res.initialRes = r0;
     if (r0 < 1e-30) { res.converged = 1; return res; }
+    // The reference's breakdown guards (|p.Ap| < 1e-30, rz + 1e-30) are
+    // absolute.  On grid meshes (above the one-CTA size) they are applied as
+    // if the system had been scaled to a unit-norm right-hand side, as the
+    // mixed engine scales it: the p' coefficients of the 2M-cell duct are so
+    // small that the absolute guard ended the CG after about 0.6 iterations
+    // per outer iteration.  One-CTA meshes (every parity case) keep the
+    // reference's absolute guards.
+    const double guard = std::is_same<T, GridTeam>::value ? 1e-30 * r0 * r0 : 1e-30;
     AmgDriver<T>::vcycle(tm, M, I);
     double a1[1] = {0.0};
     for (int c = tm.rank(); c < nC; c += tm.size()) {
@@ -426,7 +435,7 @@ __device__ __noinline__ SolveResult team_amg_pcg(T &tm, const DevMesh &M, DevIns
         }
         tm.template sum<1>(a2);
         const double pAp = a2[0];
-        if (fabs(pAp) < 1e-30) break;
+        if (fabs(pAp) < guard) break;
         const double alpha = rz / pAp;
         double a3[1] = {0.0};
         for (int c = tm.rank(); c < nC; c += tm.size()) {
@@ -446,7 +455,7 @@ __device__ __noinline__ SolveResult team_amg_pcg(T &tm, const DevMesh &M, DevIns
         for (int c = tm.rank(); c < nC; c += tm.size()) a4[0] = fma(LD(I.r + c), LD(I.s + c), a4[0]);
         tm.template sum<1>(a4);
         const double rzNew = a4[0];
-        const double beta = rzNew / (rz + 1e-30);
+        const double beta = rzNew / (rz + guard);
         for (int c = tm.rank(); c < nC; c += tm.size()) I.pv[c] = fma(beta, LD(I.pv + c), LD(I.s + c));
         tm.sync();
         rz = rzNew;
