@@ -555,22 +555,33 @@ def run_gpu(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-def run_profile_case():
-    """A bounded launch of the same kernel for profilers: 304 instances of the
-    4x128 channel (two per SM), 200 outer iterations each."""
+def run_profile_case(mesh="channel4x128"):
+    """A bounded launch of the same kernel for profilers: 304 instances (two
+    per SM) of the 4x128 channel, 200 outer iterations each, or of the
+    1920-cell permuted backward-facing step, 40 outer iterations each
+    (reference BFS settings; its FP64 solves use the reference-order AMG,
+    kernel k_simple_block_ref)."""
     import rans_sst_py as rs
     from rans_sst_py._lib import lib
-    m, bcs, nu, s = make_case_inputs()
-    s.max_iterations, s.convergence_tol = 200, 0.0
+    if mesh == "bfs1920":
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import cases as tc
+        m, bcs, nu, init = tc.bfs_case()
+        s = tc.bfs_settings(200, 0.0)
+        s.precision = PRECISION
+    else:
+        m, bcs, nu, s = make_case_inputs()
+        init = INIT
+    s.max_iterations, s.convergence_tol = (40 if mesh == "bfs1920" else 200), 0.0
     case = rs.Case(m, bcs, nu, s)
     _, coeffs, valid = theta_set()
     cf = coeffs[np.nonzero(valid)[0]]
     cf = np.concatenate([cf, cf])[:304]
-    outs = rs.solve_batch([case] * len(cf), cf, None, [INIT] * len(cf), want_state=False)
+    outs = rs.solve_batch([case] * len(cf), cf, None, [init] * len(cf), want_state=False)
     it = sum(o.iterations_run for o in outs)
     inner = sum(o.inner_iterations for o in outs)
     ms = lib().btm_last_launch_ms()
-    print(json.dumps({"profile_case": True, "instances": len(cf), "outer_iterations": it, "inner_iterations": inner,
+    print(json.dumps({"profile_case": mesh, "instances": len(cf), "outer_iterations": it, "inner_iterations": inner,
                       "launch_ms": ms, "precision": PRECISION,
                       "bytes_algorithmic": algorithmic_bytes(m.n_cells(), it, inner, PRECISION == "mixed")}))
 
@@ -845,6 +856,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="one launch of 304 instances capped at 200 outer iterations (for ncu captures)")
+    ap.add_argument("--profile-mesh", choices=["channel4x128", "bfs1920"], default="channel4x128",
+                    help="--profile-case: the mesh")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="engine of the timed arm (mixed: the batched mixed-precision form)")
     ap.add_argument("--served", action="store_true",
@@ -865,7 +878,7 @@ def main():
     PRECISION = args.precision
     world, rank, local = dist_setup()
     if args.profile_case:
-        run_profile_case()
+        run_profile_case(args.profile_mesh)
         return
     if args.c3:
         if rank == 0:
