@@ -1231,10 +1231,15 @@ int btm_case_create(const btm_mesh *mesh, const btm_patch_bc *bcs, double nu, co
                     btm_case **out) {
     if (!mesh || !settings || !out || (mesh->n_patches > 0 && !bcs)) return fail(BTM_ERR_ARG, "null argument");
     *out = nullptr;
+    // argument errors first, with or without a device
+    try {
+        check_settings(*settings);
+    } catch (const BtmError &e) {
+        return fail(e.code, e.what());
+    }
     if (int e = ensure_device()) return e;
     btm_case *C = new btm_case();
     try {
-        check_settings(*settings);
         C->nu = nu;
         C->settings = *settings;
         int blocks = 0;

@@ -53,3 +53,29 @@ def test_no_device_fails_loudly():
     bcs = rans_sst_py.FlowBoundaryConditions.channel_defaults(m, 1.0, 1e-4, 1.0)
     with pytest.raises(BtmError):
         Case(m, bcs, 1e-3, rans_sst_py.SolverSettings())
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("anderson_depth", 9, "anderson_depth"),
+    ("anderson_depth", -1, "anderson_depth"),
+    ("amg_order", 3, "amg_order"),
+    ("turb_update_interval", 0, "turb_update_interval"),
+])
+def test_settings_rejected_before_any_device_work(field, value, code):
+    """btm_case_create validates the settings (BTM_ERR_ARG, message naming
+    the field) before it looks for a device, so an invalid setting is
+    reported the same way on a machine without a GPU."""
+    import ctypes as C
+    import rans_sst_py
+    from rans_sst_py import _lib
+    m = rans_sst_py.Mesh.make_channel_2d(4, 8, 1.0, 1.0)
+    bcs = rans_sst_py.FlowBoundaryConditions.channel_defaults(m, 1.0, 1e-4, 1.0)
+    st = _lib.settings_struct(rans_sst_py.SolverSettings())
+    setattr(st, field, value)
+    md, keep_m = _lib.mesh_struct(m)
+    bca, keep_b = _lib.bc_structs(bcs)
+    L = _lib.lib()
+    h = C.c_void_p()
+    rc = L.btm_case_create(C.byref(md), bca, C.c_double(1e-3), C.byref(st), C.byref(h))
+    assert rc == -1, rc                      # BTM_ERR_ARG
+    assert code in L.btm_last_error().decode()
