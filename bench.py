@@ -592,6 +592,7 @@ SERVED_SECONDS = 10.0      # arrival window
 SERVED_CHAINS = 32
 SERVED_SEED = 13
 SERVED_MAX_ITER = 20000  # outer-iteration cap per request
+SERVED_MAX_ITER_C4 = 100000   # the same on the 2,048-cell cases
 
 
 def run_served(args):
@@ -609,14 +610,25 @@ def run_served(args):
     import cases as tc
     ps = rs.InferenceParameterSet.from_indices("c4", ACTIVE)
     base = np.array(ps.pack(rs.SSTCoefficients()))
-    m1, b1, nu1, i1 = tc.periodic_channel(32, 180.0)
-    s1 = tc.channel_settings(SERVED_MAX_ITER, TOL)
+    if args.served_cases == "c4":
+        # the configuration's 2,048-cell cases: the Re_tau 1000 channel (4x512)
+        # and the Re_tau 500 plane Couette (16x128), first cells at y+ 0.4
+        # (the 122,880-cell step of the configuration runs on the cooperative
+        # grid, about 80k outer iterations per cold solve: not served here)
+        cap = SERVED_MAX_ITER_C4
+        m1, b1, nu1, i1 = tc.periodic_channel(512, 1000.0)
+        m2, b2, nu2, i2 = tc.couette_case(16, 128)
+        names = ("channel_re1000_4x512", "couette_re500_16x128")
+    else:
+        cap = SERVED_MAX_ITER
+        m1, b1, nu1, i1 = tc.periodic_channel(32, 180.0)
+        m2, b2, nu2, i2 = tc.couette_case(4, 32)
+        names = ("channel_re180_4x32", "couette_re500_4x32")
+    s1 = tc.channel_settings(cap, TOL)
     s1.precision = "mixed"
-    m2, b2, nu2, i2 = tc.couette_case(4, 32)
-    s2 = tc.couette_settings(SERVED_MAX_ITER, TOL)
+    s2 = tc.couette_settings(cap, TOL)
     s2.precision = "mixed"
-    case_defs = [(rs.Case(m1, b1, nu1, s1), i1, "channel_re180_4x32"), (rs.Case(m2, b2, nu2, s2), i2,
-                                                                        "couette_re500_4x32")]
+    case_defs = [(rs.Case(m1, b1, nu1, s1), i1, names[0]), (rs.Case(m2, b2, nu2, s2), i2, names[1])]
     # each chain needs its likelihood: skin friction and two velocity probes,
     # evaluated on the device, are all that leaves it per request
     for cd, (m, wall) in zip(case_defs, ((m1, "bottom_wall"), (m2, "bottom_wall"))):
@@ -681,7 +693,7 @@ def run_served(args):
                        "arrival_window_s": SERVED_SECONDS, "chains": SERVED_CHAINS,
                        "cases": [cd[2] for cd in case_defs], "tol": TOL, "precision": "mixed",
                        "warm_start": "device-resident tag per chain; residuals scaled by the chain's "
-                                     "cold solve (BTM_REQ_TAG_NORMS)", "max_iterations": SERVED_MAX_ITER},
+                                     "cold solve (BTM_REQ_TAG_NORMS)", "max_iterations": cap},
             "observables": {"per_request": 3, "log_lik_finite": int(np.isfinite(lls).sum()),
                             "note": "Cf + 2 velocity probes and the log-likelihood evaluated on the device; "
                                     "no field leaves the device"},
@@ -863,6 +875,8 @@ def main():
     ap.add_argument("--served", action="store_true",
                     help="the served-stream workload (continuous batching server) instead of the batch")
     ap.add_argument("--served-rate", type=float, default=SERVED_RATE, help="served stream: arrivals per second")
+    ap.add_argument("--served-cases", choices=["small", "c4"], default="small",
+                    help="served stream: the 4x32 channel / Couette, or the configuration's 2,048-cell cases")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the plain-FP64 launch of the same batch and the error report")
     ap.add_argument("--large", choices=["bfs120k", "duct2m"], default=None,
