@@ -876,7 +876,9 @@ def main():
                     help="the served-stream workload (continuous batching server) instead of the batch")
     ap.add_argument("--served-rate", type=float, default=SERVED_RATE, help="served stream: arrivals per second")
     ap.add_argument("--served-cases", choices=["small", "c4"], default="small",
-                    help="served stream: the 4x32 channel / Couette, or the configuration's 2,048-cell cases")
+                    help="served stream: the 4x32 channel / Couette, or the configuration's 2,048-cell cases "
+                         "(c4: most requests start cold, as they arrive before their chain's previous solve "
+                         "ends; expect well over 400 s on one GPU)")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the plain-FP64 launch of the same batch and the error report")
     ap.add_argument("--large", choices=["bfs120k", "duct2m"], default=None,
