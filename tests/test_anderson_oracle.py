@@ -4,13 +4,19 @@ FP32-stored differences, FP32 Gram matrix with a 1e-6 relative Tikhonov
 term, k and omega clamped after mixing) restated around the oracle's own
 one-iteration map (oracle/simple_oracle.c, pinned bit-for-bit to the
 reference's SIMPLESolver::solve).  From the reference's state stopped at the
-1e-8 scaled residual on the Re_tau 180 4x32 channel (5e-8 from the fixed
-point), 60 accelerated iterations reach the reference's own stagnated fields
-(tests/golden/chan180_4x32.npz, 20000 iterations) to 1e-12; 60 plain
-iterations of the same map stay above 1e-8."""
+1e-8 scaled residual (the Re_tau 180 4x32 channel, 5e-8 from the fixed point;
+the periodic Couette, 1.6e-8) or from the oracle's state after 1200
+iterations (the 3-D duct, 1.2e-10), 60 accelerated iterations reach the
+reference's own stagnated fields (tests/golden/*.npz) to 1e-12; 60 plain
+iterations of the same map stay at least 30 times further away.  (Started
+much further out, 7e-3 on the duct, the accelerated iteration settles near
+2e-7 and improves only slowly while the plain one keeps contracting; the
+engine starts its histories at a scaled residual of 1e-3 and afresh in the
+FP64-assembly stage.)"""
 import json
 
 import numpy as np
+import pytest
 
 import cases
 from oracle import port
@@ -22,20 +28,38 @@ DEPTH = 8
 REG = 1e-6
 
 
-def _setup():
-    g = cases.load_golden("chan180_4x32")
+CASES = {
+    "chan180_4x32": lambda m: FlowBoundaryConditions.channel_defaults(m, 0, 0, 0),
+    "couette_4x32": lambda m: FlowBoundaryConditions.periodic_couette(m, 40.0),
+    "duct_4x16x16": lambda m: FlowBoundaryConditions.channel_defaults(m, 0, 0, 0),
+}
+DUCT_START_ITERS = 1200   # the duct golden holds no converged state: start from the oracle's
+
+
+def _setup(name):
+    g = cases.load_golden(name)
     m = cases.mesh_from_bytes(bytes(g["mesh"]))
     m.compute_wall_distance()
+    bcs = CASES[name](m)
+    nu = float(g["nu"])
     s = SolverSettings()
     for k, v in json.loads(bytes(g["settings"]).decode()).items():
         setattr(s, k, Vec3(*v) if k == "body_force" else v)
+    if "conv_U" in g:
+        x0 = {f: np.array(g["conv_" + f]) for f in FIELDS}
+    else:
+        s0 = s.copy()
+        s0.max_iterations, s0.convergence_tol = DUCT_START_ITERS, 0.0
+        a = g["init"]
+        st, _ = port.solve(m, bcs, nu, s0, cases.COEFF_DEFAULTS, 0, u=tuple(a[:3]), p=float(a[3]), k=float(a[4]),
+                           omega=float(a[5]))
+        x0 = {f: np.array(st[f]) for f in FIELDS}
+    x0["turb_established"] = 1
     # one outer iteration per call, turbulence updated from the first one
     # (the warm state has the turbulence model established)
     s.max_iterations, s.convergence_tol, s.turb_start_iter = 1, 0.0, 0
-    x0 = {f: np.array(g["conv_" + f]) for f in FIELDS}
-    x0["turb_established"] = 1
     stag = {f: np.array(g["stag_" + f]) for f in FIELDS}
-    return g, m, FlowBoundaryConditions.channel_defaults(m, 0, 0, 0), float(g["nu"]), s, x0, stag
+    return g, m, bcs, nu, s, x0, stag
 
 
 def _iterate(m, bcs, nu, s, x0, n, depth):
@@ -79,10 +103,12 @@ def _err(x, stag):
     return max(cases.rel_l2(x[f], stag[f]) for f in ("U", "k", "omega", "nuT"))
 
 
-def test_anderson_reaches_the_reference_fixed_point():
-    g, m, bcs, nu, s, x0, stag = _setup()
-    assert _err(x0, stag) > 1e-8
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_anderson_reaches_the_reference_fixed_point(name):
+    g, m, bcs, nu, s, x0, stag = _setup(name)
+    e0 = _err(x0, stag)
+    assert e0 > 1e-11
     acc = _iterate(m, bcs, nu, s, x0, 60, DEPTH)
     plain = _iterate(m, bcs, nu, s, x0, 60, 0)
-    assert _err(acc, stag) <= 1e-12, _err(acc, stag)
-    assert _err(plain, stag) > 1e-8, _err(plain, stag)
+    assert _err(acc, stag) <= 1e-12, (_err(acc, stag), e0)
+    assert _err(plain, stag) > 30 * _err(acc, stag), (_err(plain, stag), _err(acc, stag))
