@@ -330,7 +330,12 @@ int btm_solve(btm_case *c, const double *coeffs, int32_t variant,
  * extra cudaMalloc from a library would break their accounting), and
  * latency-critical loops that cannot afford cudaMalloc/cudaFree per request
  * (they can synchronise the device).  Such callers create their cases once at
- * start-up and then solve here.  Same kernel, same results as btm_solve.
+ * start-up and then solve here.  Same kernel, same results as btm_solve
+ * with the same launch shape: this call uses the CTA size the case's first
+ * btm_solve / btm_solve_batch chose (btm_case_launch_shape), and the size rule
+ * (256 threads up to 1024 cells, else 512) before any such call, since the
+ * launch-shape probe allocates; give a case one btm_solve at start-up to fix
+ * its shape.
  * The per-solve scratch lives in one static device array of 16 MiB per GPU,
  * held from library load until process exit.  Meshes above 16384 cells (the
  * one-CTA limit) and solves whose scratch plus requested residual history
@@ -416,6 +421,9 @@ int btm_wall_distance(int32_t n_cells, const double *cell_centre, int32_t n_wall
  * btm_server_poll / btm_server_flush while earlier groups still run; each
  * instance signals its own completion (a flag in mapped host memory), so a
  * slot is recycled as soon as its solve ends, not when its whole group does.
+ * A request runs with its case's launch shape (btm_case_launch_shape: the one
+ * a btm_solve / btm_solve_batch of the case chose, else the size rule), so
+ * its result is the same bits alone and among other requests.
  * warm_tag >= 0 keeps the request's final state on the device under that tag
  * and starts the next request carrying the same tag (same case) from it.
  * Results (state, history) are written into the caller's buffers, which
