@@ -273,6 +273,19 @@ def dist_setup():
     return world, rank, local
 
 
+def rank_device_env(local, env=None):
+    """The CUDA_VISIBLE_DEVICES value that gives local rank `local` its own
+    GPU, set before the process makes its first CUDA call: the rank's entry of
+    a list the launcher exported to every rank, the launcher's value when it
+    already names one device per rank, else the local rank itself."""
+    env = os.environ if env is None else env
+    vis = env.get("CUDA_VISIBLE_DEVICES")
+    if vis is None or not vis.strip():
+        return str(local)
+    ids = [v.strip() for v in vis.split(",") if v.strip()]
+    return ids[local] if len(ids) > local else vis
+
+
 def dist_barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -389,7 +402,7 @@ def run_gpu(args, world, rank, local):
     from rans_sst_py._lib import lib
 
     if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        os.environ["CUDA_VISIBLE_DEVICES"] = rank_device_env(local)
     m, bcs, nu, s = make_case_inputs()
     draws, coeffs, valid = theta_set()
     case = rs.Case(m, bcs, nu, s)

@@ -55,3 +55,18 @@ def test_two_gloo_ranks_aggregate_max_and_sum():
         assert value == pytest.approx(438.0 / 0.160)
         assert e2e_value == pytest.approx(438.0 / 0.4)
     assert out[1][5] is None
+
+
+@pytest.mark.parametrize("env,local,expect", [
+    ({}, 3, "3"),                                        # nothing exported: the local rank
+    ({"CUDA_VISIBLE_DEVICES": "0,1,2,3,4,5,6,7"}, 5, "5"),  # one list for every rank: its entry
+    ({"CUDA_VISIBLE_DEVICES": "4,5,6,7"}, 2, "6"),
+    ({"CUDA_VISIBLE_DEVICES": "6"}, 6, "6"),              # already one device per rank: kept
+    ({"CUDA_VISIBLE_DEVICES": "GPU-aa,GPU-bb"}, 1, "GPU-bb"),
+])
+def test_each_rank_gets_its_own_gpu(env, local, expect):
+    """One process per GPU: each rank restricts itself to its own device
+    before its first CUDA call, whatever list the launcher exported."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.rank_device_env(local, env) == expect
