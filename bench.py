@@ -89,7 +89,7 @@ def theta_set():
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index):
         # raw samples go next to the run's other outputs (BTM_CLOCKS_DIR, else
         # the system temporary directory); the JSON line carries the summary
         out_dir = os.environ.get("BTM_CLOCKS_DIR") or tempfile.gettempdir()
@@ -286,6 +286,15 @@ def rank_device_env(local, env=None):
     return ids[local] if len(ids) > local else vis
 
 
+def sampled_gpu(local):
+    """The nvidia-smi id (index or UUID) of the GPU this process computes on:
+    the first entry of CUDA_VISIBLE_DEVICES (nvidia-smi itself ignores that
+    variable), else the local rank."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    ids = [v.strip() for v in vis.split(",") if v.strip()] if vis else []
+    return ids[0] if ids else str(local)
+
+
 def dist_barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -425,7 +434,7 @@ def run_gpu(args, world, rank, local):
         step()
     dist_barrier(world)
     dev_ms, wall_s, conv_counts, outer, inner, fins = [], [], [], 0, 0, []
-    with ClockSampler(local) as clocks:
+    with ClockSampler(sampled_gpu(local)) as clocks:
         for _ in range(args.steps):
             outs, ms, wall = step()
             dev_ms.append(ms)
@@ -820,7 +829,7 @@ def run_c3(args):
     for _ in range(args.warmup):
         step()
     dev_ms, wall_s = [], []
-    with ClockSampler(0) as clocks:
+    with ClockSampler(sampled_gpu(0)) as clocks:
         for _ in range(args.steps):
             outs, ms, wall = step()
             dev_ms.append(ms)

@@ -70,3 +70,15 @@ def test_each_rank_gets_its_own_gpu(env, local, expect):
     sys.path.insert(0, ROOT)
     import bench
     assert bench.rank_device_env(local, env) == expect
+
+
+def test_clocks_sampled_on_the_rank_gpu(monkeypatch):
+    """The clock sampler watches the GPU the process computes on."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES", raising=False)
+    assert bench.sampled_gpu(2) == "2"
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "5")
+    assert bench.sampled_gpu(0) == "5"
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "3,4")
+    assert bench.sampled_gpu(0) == "3"
